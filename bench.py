@@ -1,0 +1,425 @@
+"""Throughput of the GB300 WCSPH-DEM step (particle-steps/s) -- one JSON line.
+
+Workload (default): the 800k-fluid variant of the large dam break -- tank
+4 x 0.8 x 1.5 m, fluid block 0.167 x 0.8 x 0.75 m at dx = 0.005 (792,000
+fluid, 2,157,576 dummy wall particles), 2,000 DEM spheres R ~ U[0.01, 0.03]
+rejection-sampled above the water, 178,528 DEM wall spheres, dt = 2.5e-5 --
+generated from seeded rules (synthetic data).  ``--workload scaled`` runs the
+dx = 0.01 dam break (100,000 fluid, 160 DEM).
+
+A step is one loop body of run_forward: moving grids re-binned + one coupled
+SPHDEM step, replayed from CUDA graphs.  value = (fluid + DEM) particles x
+steps / device time (CUDA events on the launch stream, barrier + synchronize
+on both sides, max over ranks).  The state (~200 MB at 800k) is larger than
+the 129 MB L2, so no flush is needed between steps.  e2e: the same metric
+through the public API (SPHDEM_OneStep) with the state copied from pinned host
+memory before and back after every step.  N > 1: independent replicas, one per
+GPU (the path does not shard), value = sum over ranks.
+
+``--impl reference`` times the reference algorithm on the host cores instead:
+the CPU oracle (a restatement of the reference's Warp kernels) with all
+threads, on a bounded sample of every step (every S-th subject particle),
+extrapolated to a full step by a two-point fit t(S) = F + V/S.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+FALLBACK_HBM_GBS = 6800.0
+PROFILE_DIR = ROOT / "profiles"
+
+# Algorithmic bytes per unit of each phase's kernel: every input field read
+# once, every output field written once (FP32).  Units: fluid particles unless
+# stated.  See the design doc (roofline).
+PHASE_BYTES = {
+    "force": ("fluid", 36 + 24),          # pos, vel, m, rho, pres in; acc, pgf out
+    "density": ("fluid", 20 + 8),         # pos, m, flt in; rho, pres out
+    "wall_density": ("wall", 16 + 8),     # pos, m in; rho, pres out (per wall particle)
+    "porosity": ("fluid", 20 + 4),        # pos, m, rho in; porosity out
+    "grid_sph": ("fluid", 12 + 8 + 32 + 36),  # bin pos; key+order; gather in; sorted out
+    "react_integrate": ("fluid", 44 + 48),
+    "exchange": ("dem", 176),
+    "contacts": ("dem", 176),
+    "grid_dem": ("dem", 20),
+    "dem_step": ("dem", 72 + 48),
+}
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def make_case(workload: str, device):
+    from warp_sph_gpt_gb300.generate import build_case, config_large, config_scaled, solver_config
+
+    if workload == "large800k":
+        gen, pos, rad = config_large(fluid_width=0.167, seed=0, n_dem=2000)
+        desc = ("large dam break, 800k variant: tank 4x0.8x1.5 m, fluid 0.167x0.8x0.75 m at dx=0.005, "
+                "2,000 DEM R~U[0.01,0.03], dt=2.5e-5")
+    elif workload == "scaled":
+        gen, pos, rad = config_scaled(seed=0)
+        desc = "scaled dam break: tank 2x0.4x1 m, fluid 0.5x0.4x0.5 m at dx=0.01, 160 DEM R=0.025, dt=5e-5"
+    else:
+        raise SystemExit(f"unknown workload {workload}")
+    P, B, D, W = build_case(gen, pos, rad, device=device)
+    solv = solver_config(gen)
+    return gen, solv, (P, B, D, W), desc
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.proc = None
+        self.gpu = gpu_index
+        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+
+    def __enter__(self):
+        try:
+            self.path.parent.mkdir(exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.gpu), "-lms", "100"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+            time.sleep(0.3)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.2)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if self.proc is None or not self.path.exists():
+            return None
+        rows = []
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def peak_hbm():
+    try:
+        peaks = json.loads(PEAKS_FILE.read_text())
+        return float(peaks["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+def profile_traffic(kernel: str, workload: str):
+    """Per-launch DRAM bytes from the committed ncu summary, if present."""
+    for p in PROFILE_DIR.glob(f"*{kernel}*{workload}*.txt"):
+        for line in p.read_text().splitlines():
+            if line.startswith("traffic_bytes_per_launch:"):
+                try:
+                    return float(line.split(":", 1)[1])
+                except ValueError:
+                    pass
+    return None
+
+
+def gpu_arm(args, rank, world, local_rank):
+    import torch
+    import torch.distributed as dist
+    import ctypes as C
+
+    from warp_sph_gpt_gb300 import HashGrid, SPHDEM_OneStep, dem_search_scales, run_steps
+    from warp_sph_gpt_gb300 import _lib
+    from warp_sph_gpt_gb300.engine import context_for
+
+    torch.cuda.set_device(local_rank)
+    device = torch.device("cuda", local_rank)
+    gen, solv, (P, B, D, W), desc = make_case(args.workload, device)
+    scales = dem_search_scales(D, W)
+    grids = [HashGrid() for _ in range(4)]
+    grids[0].build(P.pos, solv.support)
+    grids[1].build(B.pos, solv.support)
+    grids[2].build(D.pos, max(2.0 * scales[0], 2.0 * scales[2]))
+    grids[3].build(W.pos, max(2.0 * scales[1], solv.support))
+    n_units = P.n + D.n
+    log(f"[rank {rank}] {desc}: fluid {P.n}, wall {B.n}, DEM {D.n}, DEM wall {W.n}")
+
+    # warm-up (also captures the graphs)
+    run_steps(solv, P, B, grids[0], grids[1], D, W, grids[2], grids[3], first_step=0, n_steps=args.warmup,
+              search_scales=scales)
+    torch.cuda.synchronize()
+    ctx = context_for(P, B, D, W, tuple(grids))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    stream = torch.cuda.current_stream()
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        start.record(stream)
+        run_steps(solv, P, B, grids[0], grids[1], D, W, grids[2], grids[3], first_step=args.warmup,
+                  n_steps=args.steps, search_scales=scales)
+        end.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = start.elapsed_time(end)
+    first = args.warmup
+    shep = sum(1 for s in range(first, first + args.steps) if s == 0 or s % solv.shepard_step == 0)
+    k1 = ctx.lib.sphdem_graph_kernels(C.byref(ctx.ctx), 1)
+    k0 = ctx.lib.sphdem_graph_kernels(C.byref(ctx.ctx), 0)
+    launches = shep * max(k1, 0) + (args.steps - shep) * max(k0, 0)
+    ms_max = ms
+    if world > 1:
+        t = torch.tensor([ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_max = float(t.item())
+    ctx.check_status()
+
+    # per-phase device times (CUDA events between phases, same stream)
+    phase_ms = np.zeros(len(_lib.PHASES))
+    reps = 5
+    buf = (C.c_float * len(_lib.PHASES))()
+    for r in range(reps):
+        ctx.prepare(rebuild_moving=False)
+        _lib.check(ctx.lib.sphdem_profile_step(C.byref(ctx.ctx), C.byref(ctx.params), first + args.steps + r, 1,
+                                               buf, ctx.stream), "profile")
+        D._flip("dem")  # the profiled step swapped both contact CSRs on the device
+        D._flip("bnd")
+        phase_ms += np.array(buf[:])
+    phase_ms /= reps
+    phases = {name: round(float(v), 4) for name, v in zip(_lib.PHASES, phase_ms)}
+    dom = max(phases, key=phases.get)
+    unit, per = PHASE_BYTES.get(dom, ("fluid", 0))
+    units = {"fluid": P.n, "wall": B.n, "dem": D.n}[unit]
+    alg_bytes = per * units
+    peak, peak_kind = peak_hbm()
+    achieved = alg_bytes / (phases[dom] * 1e-3) / 1e9 if phases[dom] > 0 else 0.0
+
+    # e2e through the public API with host buffers
+    e2e_steps = min(args.steps, args.e2e_steps)
+    host = {k: torch.empty_like(t, device="cpu").pin_memory() for k, t in
+            (("pos", P.pos), ("vel", P.vel), ("dpos", D.pos), ("dvel", D.vel), ("domega", D.omega))}
+    for k, t in (("pos", P.pos), ("vel", P.vel), ("dpos", D.pos), ("dvel", D.vel), ("domega", D.omega)):
+        host[k].copy_(t)
+    h2d = sum(t.numel() * t.element_size() for t in host.values())
+    d2h = h2d
+    torch.cuda.synchronize()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for s in range(e2e_steps):
+        P.pos.copy_(host["pos"], non_blocking=True)
+        P.vel.copy_(host["vel"], non_blocking=True)
+        D.pos.copy_(host["dpos"], non_blocking=True)
+        D.vel.copy_(host["dvel"], non_blocking=True)
+        D.omega.copy_(host["domega"], non_blocking=True)
+        SPHDEM_OneStep(solv, P, B, D, W, *grids, first + args.steps + reps + s, scales)
+        host["pos"].copy_(P.pos, non_blocking=True)
+        host["vel"].copy_(P.vel, non_blocking=True)
+        host["dpos"].copy_(D.pos, non_blocking=True)
+        host["dvel"].copy_(D.vel, non_blocking=True)
+        host["domega"].copy_(D.omega, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if world > 1:
+        t = torch.tensor([e2e_ms], device=device)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+
+    result = {
+        "metric": "particle-steps/s",
+        "value": world * n_units * args.steps / (ms_max * 1e-3),
+        "unit": "particle-steps/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms_max / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded generator rules of the reference's input_gen)",
+        "config": {"workload": desc, "fluid": P.n, "wall": B.n, "dem": D.n, "dem_wall": W.n,
+                   "particles_counted": "fluid + moving DEM", "parallelism": f"replicas x{world}",
+                   "l2": "state > 129 MB L2 (no flush)" if args.workload == "large800k"
+                   else "state < L2 (resident between steps, as in a run)"},
+        "e2e": {"value": world * n_units * e2e_steps / (e2e_ms * 1e-3), "unit": "particle-steps/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
+                "api": "SPHDEM_OneStep per step, state copied from / to pinned host memory"},
+        "roofline": {"bound": "hbm", "kernel_phase": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": alg_bytes,
+                     "traffic": profile_traffic(dom, args.workload)},
+        "phases_ms": phases,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        result["cpu_baseline"] = cpu_baseline(gen, solv, (P, B, D, W), scales, args.cpu_budget_s)
+    return result
+
+
+# ---------------------------------------------------------------------------
+# CPU (reference algorithm) timing
+# ---------------------------------------------------------------------------
+def _oracle_state(parts):
+    from oracle.oracle import HostState
+
+    return HostState(*parts)
+
+
+def cpu_sample(host, solv, scales, stride: int, step: int) -> float:
+    from oracle import oracle as O
+
+    O.set_subject_stride(stride)
+    t0 = time.perf_counter()
+    host.sphdem_onestep(solv, step, scales, p="f32")
+    dt = time.perf_counter() - t0
+    O.set_subject_stride(1)
+    return dt
+
+
+def cpu_fit(host, solv, scales, budget_s: float):
+    """Choose a subject stride S so one sample fits the budget, then fit the
+    full-step time F + V from samples at S and 2S."""
+    n = len(host.sph["pos"])
+    stride = max(1, n // 2048)
+    t = cpu_sample(host, solv, scales, stride, 1)
+    # aim one sample at ~budget/4
+    while t < budget_s / 8 and stride > 1:
+        stride = max(1, stride // 2)
+        t = cpu_sample(host, solv, scales, stride, 1)
+    t1 = cpu_sample(host, solv, scales, stride, 1)
+    t2 = cpu_sample(host, solv, scales, 2 * stride, 1) if stride * 2 <= n else t1
+    V = max(0.0, 2 * stride * (t1 - t2)) if stride > 1 else t1
+    F = max(0.0, t1 - V / stride)
+    return stride, t1, t2, F + V
+
+
+def cpu_baseline(gen, solv, parts, scales, budget_s):
+    from oracle import oracle as O
+
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    O.set_threads(cores)
+    host = _oracle_state(parts)
+    stride, t1, t2, full = cpu_fit(host, solv, scales, budget_s)
+    n_units = len(host.sph["pos"]) + len(host.dem["pos"])
+    return {"value": n_units / full, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "sample": f"CPU oracle (restatement of the reference Warp kernels, FP32) on {cores} threads: one coupled "
+                      f"step on every {stride}-th and every {2 * stride}-th subject particle ({t1:.2f} s, {t2:.2f} s), "
+                      f"full step {full:.2f} s from the fit t(S) = F + V/S"}
+
+
+def reference_arm(args):
+    """--impl reference: the reference algorithm on the host cores."""
+    from oracle import oracle as O
+
+    gen, solv, parts, desc = make_case(args.workload, "cpu")
+    from warp_sph_gpt_gb300 import dem_search_scales
+
+    scales = dem_search_scales(parts[2], parts[3])
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+    O.set_threads(cores)
+    host = _oracle_state(parts)
+    n_units = parts[0].n + parts[2].n
+    stride, t1, t2, full = cpu_fit(host, solv, scales, args.cpu_budget_s)
+    samples = []
+    for s in range(args.warmup + args.steps):
+        t = cpu_sample(host, solv, scales, stride, 1 + s)
+        if s >= args.warmup:
+            samples.append(t)
+    mean_sample = statistics.mean(samples) if samples else t1
+    scale = full / t1 if t1 > 0 else 1.0  # sample -> full step
+    step_s = mean_sample * scale
+    value = n_units / step_s
+    return {"impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
+            "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded generator rules of the reference's input_gen)",
+            "config": {"workload": desc, "fluid": parts[0].n, "wall": parts[1].n, "dem": parts[2].n,
+                       "dem_wall": parts[3].n},
+            "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+                             "sample": f"every {stride}-th subject per step, scaled by the fit F + V/S "
+                                       f"(full step {full:.2f} s)"},
+            "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
+    ap.add_argument("--workload", default="large800k", choices=("large800k", "scaled"))
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-budget-s", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        print(json.dumps(reference_arm(args)), flush=True)
+        return
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", init_method="env://")
+    result = gpu_arm(args, rank, world, local_rank)
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

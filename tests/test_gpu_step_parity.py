@@ -1,0 +1,252 @@
+"""GPU parity of the coupled step against the CPU oracle.
+
+Tolerances (stated once, used throughout):
+* neighbour sets and contact CSR (offsets, ids): bit-exact against the FP32
+  oracle (reference semantics);
+* whole-step fields: the GPU must be no further from the FP64 oracle than the
+  FP32 oracle itself (the reference's own arithmetic) is, within a factor 4,
+  with a 1e-5 floor:  err(gpu, f64) <= max(1e-5, 4 err(f32, f64)), where err is
+  the field-normalised max|a - b| / max|b|.  A whole step chains density ->
+  Tait pressure -> force, and near rest B((rho/rho0)^7 - 1) amplifies the
+  ~1e-7 FP32 density rounding by the EOS condition number, so a fixed 1e-5 on
+  acceleration is not reachable by any FP32 evaluation (the FP32 oracle misses
+  it too); pressure is normalised by the bulk modulus K = rho0 c0^2.
+  Each kernel on its own meets 1e-5 against FP64 on shared inputs
+  (tests/test_gpu_kernels.py).
+"""
+import numpy as np
+import pytest
+import torch
+
+from helpers import assign, contact_history, field_err, run_bc_dem, run_force_dem, scene
+from oracle.oracle import HostState
+from warp_sph_gpt_gb300 import HashGrid, SPH_OneStep, SPHDEM_OneStep, dem_search_scales
+from warp_sph_gpt_gb300.generate import DamPtlGeneration
+from warp_sph_gpt_gb300.kernels import Kernel_step_dem, neighbour_digest
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-5
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def _err(got, ref, scale_floor=0.0):
+    got = np.asarray(got, np.float64)
+    ref = np.asarray(ref, np.float64)
+    if ref.size == 0:
+        return 0.0
+    return float(np.abs(got - ref).max() / max(np.abs(ref).max(), scale_floor, 1e-30))
+
+
+def _compare_step(s, P, B, D, h32, h64, tol=FIELD_TOL, factor=4.0):
+    bulk = s.rho0 * s.c0 ** 2
+    bad = {}
+    groups = (("sph", P, ("rho", "pres", "acc", "pos", "vel", "porosity", "pgf", "acc_dem", "flt")),
+              ("bnd", B, ("rho", "pres")),
+              ("dem", D, ("force", "torque", "pos", "vel", "omega", "flt_s", "porosity", "drag", "pressure_force")))
+    for group, obj, names in groups:
+        for name in names:
+            floor = bulk if name == "pres" else 0.0
+            r64 = getattr(h64, group)[name]
+            e_gpu = _err(_np(getattr(obj, name)), r64, floor)
+            e_ref = _err(getattr(h32, group)[name], r64, floor)
+            if not e_gpu <= max(tol, factor * e_ref):
+                bad[f"{group}.{name}"] = (e_gpu, e_ref)
+    assert not bad, f"fields beyond max({tol}, {factor} x FP32-oracle error): {bad}"
+
+
+def _compare_csr(D, host):
+    for kind in ("dem", "bnd"):
+        ref = host.side(kind, "old")
+        off = _np(getattr(D, f"contact_{kind}_offset_old"))
+        np.testing.assert_array_equal(off, ref["offset"], err_msg=f"{kind} offsets")
+        np.testing.assert_array_equal(_np(getattr(D, f"contact_{kind}_id_old")), ref["id"], err_msg=f"{kind} ids")
+        tang = _np(getattr(D, f"tang_{kind}_old"))
+        if len(tang):
+            assert field_err(tang, ref["tang"]) < 1e-5, f"{kind} tangential history"
+
+
+@pytest.mark.parametrize("origin_z", [0.2, 0.60])
+def test_coupled_steps_match_fp64_oracle(origin_z):
+    """Per-step fields against the FP64 oracle, CSR against the FP32 oracle."""
+    s, P, B, D, DB, grids = scene(dem_nx=3, dem_ny=2, dem_origin_x=0.1, dem_origin_y=0.1, dem_spacing=0.05,
+                                  dem_origin_z=origin_z)
+    scales = dem_search_scales(D, DB)
+    for step in range(4):
+        h64 = HostState(P, B, D, DB)
+        h32 = HostState(P, B, D, DB)
+        grids[0].build(P.pos, s.support)
+        grids[2].build(D.pos, s.dem_support)
+        SPHDEM_OneStep(s, P, B, D, DB, *grids, step, scales)
+        torch.cuda.synchronize()
+        h64.sphdem_onestep(s, step, scales, p="f64")
+        h32.sphdem_onestep(s, step, scales, p="f32")
+        _compare_step(s, P, B, D, h32, h64)
+        _compare_csr(D, h32)
+
+
+RELATIONS = ["SPH_SPH_SUPPORT", "SPH_BND_SUPPORT", "BND_SPH_SUPPORT", "BND_BND_SUPPORT", "SPH_SPH_FORCE",
+             "SPH_BND_FORCE", "SPH_SPH_LEN", "SPH_DEM_2H", "DEM_SPH_2H", "DEM_DEM_2H", "SPH_DEM_REACT"]
+
+
+@pytest.mark.parametrize("relation", RELATIONS)
+def test_neighbour_sets_bit_exact(relation):
+    """Every neighbour relation of the step, per subject, equals the FP32
+    oracle's: member count and an order-independent hash of the member ids."""
+    s, P, B, D, DB, grids = scene(dem_nx=3, dem_ny=2, dem_origin_x=0.1, dem_origin_y=0.1, dem_spacing=0.05,
+                                  dem_origin_z=0.2)
+    scales = dem_search_scales(D, DB)
+    # advance a few steps so positions are off the lattice
+    for step in range(3):
+        SPHDEM_OneStep(s, P, B, D, DB, *grids, step, scales)
+    radius = s.support if "SUPPORT" in relation or "FORCE" in relation else 2.0 * scales[2]
+    got_c, got_h = neighbour_digest(relation, radius, P, B, D, grids[:3] + [None])
+    host = HostState(P, B, D, DB)
+    ref_c, ref_h = host.neighbour_digest(relation, radius)
+    np.testing.assert_array_equal(_np(got_c), ref_c)
+    np.testing.assert_array_equal(_np(got_h).view(np.uint64), ref_h)
+    assert ref_c.sum() > 0 or relation in ("SPH_DEM_REACT",)
+
+
+def test_dry_free_fall_is_bit_identical_to_sph_only():
+    """Coupled step with far-away DEM == SPH-only step, bit for bit; DEM falls
+    freely (tests/test_dem.py:574-597)."""
+    s, P, B, D, DB, grids = scene(dem_origin_z=1.5)
+    P0, B0 = DamPtlGeneration(s).build("cuda")
+    gs, gb = HashGrid(32, 32, 32), HashGrid(32, 32, 32)
+    gb.build(B0.pos, s.support)
+    initial = _np(D.pos).copy()
+    for step in range(5):
+        grids[0].build(P.pos, s.support)
+        grids[2].build(D.pos, s.dem_support)
+        gs.build(P0.pos, s.support)
+        SPH_OneStep(s, P0, B0, gs, gb, step)
+        SPHDEM_OneStep(s, P, B, D, DB, *grids, step)
+    np.testing.assert_array_equal(_np(P.pos), _np(P0.pos))
+    np.testing.assert_array_equal(_np(P.vel), _np(P0.vel))
+    np.testing.assert_array_equal(_np(D.vel)[:, :2], 0.0)
+    np.testing.assert_allclose(_np(D.vel)[:, 2], -5 * s.g * s.dt, rtol=1e-6)
+    np.testing.assert_allclose(_np(D.pos)[:, 2], initial[:, 2] - s.g * s.dt ** 2 * 15, atol=5e-7)
+
+
+def test_compact_csr_rows_store_all_stable_directed_ids():
+    """tests/test_dem.py:199-216: three coincident spheres, rows {0,1,2}\\{a}."""
+    s, P, B, D, DB, grids = scene(dem_nx=3)
+    D.pos[:] = torch.tensor([0.3, 0.16, 0.6])
+    grids[2].build(D.pos, s.dem_support)
+    count = run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt)
+    offsets = _np(D.contact_dem_offset_old)
+    ids = _np(D.contact_dem_id_old)
+    assert count == 6 and int(offsets[-1]) == 6
+    assert D.contact_dem_id_old.shape == (6,) and D.tang_dem_old.shape == (6, 3)
+    np.testing.assert_array_equal(np.diff(offsets), [2, 2, 2])
+    for a in range(3):
+        assert set(map(int, ids[offsets[a]:offsets[a + 1]])) == {0, 1, 2} - {a}
+
+
+def test_csr_grows_shrinks_to_zero_and_recontact_starts_fresh():
+    """0 -> 2 -> 6 -> 2 -> 0 -> 2 with survivor history (tests/test_dem.py:218-286)."""
+    s, P, B, D, DB, grids = scene(dem_nx=3)
+    assert run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt) == 0
+    assert D.contact_dem_id_old.shape == (0,)
+    pair = [[0.200, 0.16, 0.60], [0.249, 0.16, 0.60], [0.600, 0.16, 0.60]]
+    assign(D.pos, pair)
+    assign(D.vel, [[0, 0, 0], [0, 0.01, 0], [0, 0, 0]])
+    grids[2].build(D.pos, s.dem_support)
+    assert run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt) == 2
+    first = contact_history(D, "dem", 0, 1).copy()
+    assert D.contact_dem_id_new.shape == (0,)
+    D.pos[:] = torch.tensor([0.3, 0.16, 0.6])
+    grids[2].build(D.pos, s.dem_support)
+    assert run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt) == 6
+    assert D.contact_dem_id_new.shape == (2,)
+    assign(D.pos, pair)
+    grids[2].build(D.pos, s.dem_support)
+    assert run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt) == 2
+    np.testing.assert_allclose(contact_history(D, "dem", 0, 1), 3.0 * first, rtol=1e-6, atol=1e-9)
+    assign(D.pos, [[0.1, 0.16, 0.60], [0.4, 0.16, 0.60], [0.7, 0.16, 0.60]])
+    grids[2].build(D.pos, s.dem_support)
+    assert run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt) == 0
+    assign(D.pos, pair)
+    grids[2].build(D.pos, s.dem_support)
+    assert run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt) == 2
+    np.testing.assert_allclose(contact_history(D, "dem", 0, 1), first, rtol=1e-6, atol=1e-9)
+
+
+def test_normal_contact_and_release_history():
+    """F = K 0.001 + eta 2 along x, pair sum 0, release clears history
+    (tests/test_dem.py:386-416)."""
+    s, P, B, D, DB, grids = scene(dem_nx=2, dem_ny=1)
+    assign(D.pos, [[0.2, 0.16, 0.6], [0.249, 0.16, 0.6]])
+    assign(D.vel, [[1, 0, 0], [-1, 0, 0]])
+    grids[2].build(D.pos, s.dem_support)
+    run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt)
+    expected = s.dem_K * 0.001 + s.dem_eta * 2
+    np.testing.assert_allclose(_np(D.force), [[-expected, 0, 0], [expected, 0, 0]], rtol=2e-5, atol=0.01)
+    np.testing.assert_allclose(_np(D.force).sum(axis=0), 0, atol=1e-6)
+    D.tang_dem_old[:] = torch.tensor([0.0, 0.1, 0.0])
+    assign(D.pos, [[0.2, 0.16, 0.6], [1.5, 0.16, 0.6]])
+    grids[2].build(D.pos, s.dem_support)
+    run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt)
+    assert int(D.contact_dem_offset_old[-1]) == 0
+    np.testing.assert_array_equal(_np(D.force), 0)
+    assign(D.pos, [[0.2, 0.16, 0.6], [0.249, 0.16, 0.6]])
+    assign(D.vel, [[0, 0, 0], [0, 0.01, 0]])
+    grids[2].build(D.pos, s.dem_support)
+    run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt)
+    assert abs(float(contact_history(D, "dem", 0, 1)[1]) - 0.01 * s.dt) < 1e-8
+
+
+def test_friction_history_and_spin():
+    """Sticking displacement grows linearly, lever 0.0245, spin, Coulomb limit
+    (tests/test_dem.py:418-444)."""
+    s, P, B, D, DB, grids = scene(dem_nx=2, dem_ny=1)
+    assign(D.pos, [[0.2, 0.16, 0.6], [0.249, 0.16, 0.6]])
+    assign(D.vel, [[0, 0, 0], [0, 0.01, 0]])
+    grids[2].build(D.pos, s.dem_support)
+    for count in (1, 2):
+        run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt)
+        tangential = s.dem_K * 0.01 * s.dt * count + s.dem_eta * 0.01
+        assert abs(float(D.force[0, 1]) - tangential) < 1e-5
+        assert abs(float(contact_history(D, "dem", 0, 1)[1]) - count * 0.01 * s.dt) < 1e-8
+    torque = _np(D.torque)
+    np.testing.assert_allclose(torque[:, 2], 0.0245 * tangential, rtol=1e-5)
+    Kernel_step_dem(D, s.dt)
+    np.testing.assert_allclose(_np(D.omega)[:, 2], torque[:, 2] / s.dem_inertia * s.dt, rtol=1e-5)
+    assign(D.vel, [[0, 0, 0], [0, 10, 0]])
+    D.omega.zero_()
+    assign(D.pos, [[0.2, 0.16, 0.6], [0.249, 0.16, 0.6]])
+    grids[2].build(D.pos, s.dem_support)
+    run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt)
+    assert abs(float(D.force[0, 1]) - s.dem_mu * s.dem_K * 0.001) < 0.01
+
+
+def test_fixed_boundary_contact_and_release():
+    """Wall contact count > 0, history, +z force, release and fresh recontact
+    (tests/test_dem.py:446-492)."""
+    s, P, B, D, DB, grids = scene(dem_nx=1, dem_ny=1)
+    contact_pos = [[0.4, 0.16, 0.020]]
+    assign(D.pos, contact_pos)
+    D.vel[:] = torch.tensor([0.1, 0.0, -0.2])
+    grids[2].build(D.pos, s.dem_support)
+    run_force_dem(D, grids[2], s.dem_radius, 0.0, s.dt)
+    fixed = _np(DB.pos).copy()
+    n = run_bc_dem(D, DB, grids[3], s.dem_bnd_radius, s.dt)
+    assert n > 0 and D.contact_bnd_id_old.shape == (n,)
+    first_neighbour = int(D.contact_bnd_id_old[0])
+    first_history = contact_history(D, "bnd", 0, first_neighbour).copy()
+    assert np.linalg.norm(first_history) > 0
+    assert float(D.force[0, 2]) > 0 and float(D.torque[0].norm()) > 0
+    Kernel_step_dem(D, s.dt)
+    np.testing.assert_array_equal(_np(DB.pos), fixed)
+    D.pos[:] = torch.tensor([0.4, 0.16, 0.8])
+    run_bc_dem(D, DB, grids[3], s.dem_bnd_radius, s.dt)
+    assert int(D.contact_bnd_offset_old[-1]) == 0
+    assign(D.pos, contact_pos)
+    D.vel[:] = torch.tensor([0.1, 0.0, -0.2])
+    D.omega.zero_()
+    run_bc_dem(D, DB, grids[3], s.dem_bnd_radius, s.dt)
+    np.testing.assert_allclose(contact_history(D, "bnd", 0, first_neighbour), first_history, rtol=1e-6, atol=1e-9)

@@ -1,0 +1,343 @@
+// sph.cu -- WCSPH neighbour loops on the sorted fluid / wall copies.
+//
+// One thread per subject, subjects taken in cell order (grid order), so the
+// threads of a warp query the same few cell columns and their float4
+// neighbour loads hit the same L1 lines.  Neighbour membership uses the exact
+// FP32 predicates of the reference; the physics sums use contracted FP32.
+//
+//   k_density        Kernel_shepard_sph + Kernel_density_sph + Kernel_pres_sph
+//                    (kernel/KERNEL_rho.py:6-82, kernel/KERNEL_pres.py:6-23) in
+//                    one pass: the Shepard sum, when due, shares the loop.
+//   k_density_wall   Kernel_density_bnd + Kernel_pres_bnd (KERNEL_rho.py:87-126,
+//                    KERNEL_pres.py:26-45) with the constant wall-wall part cached.
+//   k_force          Kernel_force_sph (kernel/KERNEL_force.py:7-71) and the
+//                    pressure-gradient half of Kernel_prep_sphdem
+//                    (kernel/KERNEL_SPHDEM_interaction.py:97-112): same
+//                    neighbours, same support, one loop.
+//   k_step_sph       Kernel_step_sph (kernel/KERNEL_step.py:6-22).
+#include "common.cuh"
+
+namespace sd {
+
+namespace {
+
+struct DensArgs {
+    Geo gs, gb;
+    const float4* __restrict__ f_posm;
+    const float* __restrict__ f_vprev;  // m/rho before this pass (Shepard input)
+    const float4* __restrict__ b_posm;
+    const float* __restrict__ b_vprev;
+    float* flt;
+    float* rho;
+    float* pres;
+    float4* f_rp;    // out: rho, pres, pres/rho^2, 1/rho  (sorted)
+    float4* f_posv;  // out: x, y, z, m/rho                 (sorted)
+    int n;
+    float s2, rq;
+    Kern kern;
+    float rho0, B, gamma;
+};
+
+template <bool FLT, bool RHO, bool PRES>
+__global__ void __launch_bounds__(128) k_density(DensArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const int o = a.gs.order[k];
+    const float4 p = a.f_posm[k];
+    const int inst = inst_of(a.gs, o);
+    float rho_sum = 0.0f, flt_sum = 0.0f;
+    const Win ws = window(a.gs, p.x, p.y, p.z, a.rq);
+    for_each_range(a.gs, ws, inst, [&](int s, int e) {
+        for (int j = s; j < e; ++j) {
+            const float4 q = a.f_posm[j];
+            const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+            if (r.d2 < a.s2) {
+                const float w = kern_w(a.kern, fast_sqrt(r.d2));
+                if (RHO) rho_sum += q.w * w;
+                if (FLT) flt_sum += a.f_vprev[j] * w;
+            }
+        }
+    });
+    if (a.gb.ncl > 0) {
+        const Win wb = window(a.gb, p.x, p.y, p.z, a.rq);
+        for_each_range(a.gb, wb, inst, [&](int s, int e) {
+            for (int j = s; j < e; ++j) {
+                const float4 q = a.b_posm[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 < a.s2) {
+                    const float w = kern_w(a.kern, fast_sqrt(r.d2));
+                    if (RHO) rho_sum += q.w * w;
+                    if (FLT) flt_sum += a.b_vprev[j] * w;
+                }
+            }
+        });
+    }
+    if (FLT) a.flt[o] = flt_sum;
+    if (RHO) {
+        const float flt = FLT ? flt_sum : a.flt[o];
+        const float rho = rho_sum / flt;
+        a.rho[o] = rho;
+        if (PRES) {
+            const float pr = tait(rho, a.rho0, a.B, a.gamma);
+            a.pres[o] = pr;
+            const float irho = 1.0f / rho;
+            a.f_rp[k] = make_float4(rho, pr, pr * irho * irho, irho);
+            a.f_posv[k] = make_float4(p.x, p.y, p.z, p.w * irho);
+        }
+    }
+}
+
+struct WallArgs {
+    Geo gs, gb;
+    const float4* __restrict__ f_posm;
+    const float4* __restrict__ b_posm;
+    const float* __restrict__ b_self;
+    float* rho;
+    float* pres;
+    float4* b_rp;
+    int n;
+    float s2, rq;
+    Kern kern;
+    float rho0, B, gamma;
+};
+
+template <bool PRES>
+__global__ void __launch_bounds__(128) k_density_wall(WallArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const int o = a.gb.order[k];
+    const float4 p = a.b_posm[k];
+    const int inst = inst_of(a.gb, o);
+    float rho_sum = 0.0f;
+    if (a.gs.ncl > 0) {
+        const Win ws = window(a.gs, p.x, p.y, p.z, a.rq);
+        for_each_range(a.gs, ws, inst, [&](int s, int e) {
+            for (int j = s; j < e; ++j) {
+                const float4 q = a.f_posm[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 < a.s2) rho_sum += q.w * kern_w(a.kern, fast_sqrt(r.d2));
+            }
+        });
+    }
+    const float rho = rho_sum + a.b_self[k];
+    a.rho[o] = rho;
+    if (PRES) {
+        const float pr = tait(rho, a.rho0, a.B, a.gamma);
+        a.pres[o] = pr;
+        const float irho = 1.0f / rho;
+        a.b_rp[k] = make_float4(rho, pr, pr * irho * irho, irho);
+    }
+}
+
+struct ForceArgs {
+    Geo gs, gb;
+    const float4* __restrict__ f_posm;
+    const float4* __restrict__ f_vel;
+    const float4* __restrict__ f_rp;
+    const float4* __restrict__ b_posm;
+    const float4* __restrict__ b_vel;
+    const float4* __restrict__ b_rp;
+    float* acc;
+    float* pgf;
+    float4* f_pgf;  // out (sorted): pgf x, y, z, rho
+    int n;
+    float s2, rq;
+    Kern kern;
+    float two_mu, eps_h2, g;
+};
+
+// Pair term shared by the fluid and wall loops.  MODE bit 1: acceleration,
+// bit 2: negative pressure gradient.
+template <int MODE>
+__device__ __forceinline__ void force_pair(const ForceArgs& a, const D2& r, const float4& vi, float pr_i,
+                                           float p_i, float irho_i, const float4& q, const float4& rpj,
+                                           const float4* __restrict__ velp, int j, float3& acc, float3& pgf) {
+    const float rinv = rsqrtf(r.d2);
+    const float dist = r.d2 * rinv;
+    const float dwr = kern_dw(a.kern, dist) * rinv;  // (dW/dr) / r
+    const float gx = dwr * r.dx, gy = dwr * r.dy, gz = dwr * r.dz;  // grad_i W
+    if (MODE & 1) {
+        const float sc = q.w * (pr_i + rpj.z);
+        const float4 vj = velp[j];
+        const float visc =
+            __fdividef(a.two_mu * (r.dx * gx + r.dy * gy + r.dz * gz) * irho_i * rpj.w, r.d2 + a.eps_h2);
+        const float mv = q.w * visc;
+        acc.x += mv * (vi.x - vj.x) - sc * gx;
+        acc.y += mv * (vi.y - vj.y) - sc * gy;
+        acc.z += mv * (vi.z - vj.z) - sc * gz;
+    }
+    if (MODE & 2) {
+        const float c = q.w * rpj.w * (rpj.y - p_i);
+        pgf.x -= c * gx;
+        pgf.y -= c * gy;
+        pgf.z -= c * gz;
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) k_force(ForceArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const int o = a.gs.order[k];
+    const float4 p = a.f_posm[k];
+    const float4 vi = a.f_vel[k];
+    const float4 rpi = a.f_rp[k];
+    const int inst = inst_of(a.gs, o);
+    float3 acc = make_float3(0.f, 0.f, 0.f), pgf = make_float3(0.f, 0.f, 0.f);
+    const Win ws = window(a.gs, p.x, p.y, p.z, a.rq);
+    for_each_range(a.gs, ws, inst, [&](int s, int e) {
+        for (int j = s; j < e; ++j) {
+            const float4 q = a.f_posm[j];
+            const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+            if (r.d2 > kR2Min && r.d2 < a.s2)
+                force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.f_rp[j], a.f_vel, j, acc, pgf);
+        }
+    });
+    if (a.gb.ncl > 0) {
+        const Win wb = window(a.gb, p.x, p.y, p.z, a.rq);
+        for_each_range(a.gb, wb, inst, [&](int s, int e) {
+            for (int j = s; j < e; ++j) {
+                const float4 q = a.b_posm[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 > kR2Min && r.d2 < a.s2)
+                    force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.b_rp[j], a.b_vel, j, acc, pgf);
+            }
+        });
+    }
+    if (MODE & 1) st3(a.acc, o, make_float3(acc.x, acc.y, acc.z - a.g));
+    if (MODE & 2) {
+        if (a.pgf) st3(a.pgf, o, pgf);
+        a.f_pgf[k] = make_float4(pgf.x, pgf.y, pgf.z, rpi.x);
+    }
+}
+
+__global__ void k_pres(const float* __restrict__ rho, float* __restrict__ pres, int n, float rho0, float B,
+                       float gamma) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) pres[i] = tait(rho[i], rho0, B, gamma);
+}
+
+}  // namespace
+
+namespace {
+__global__ void k_step_sph(float* pos, float* vel, const float* __restrict__ acc, int n, float dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) euler_store(pos, vel, i, ld3(acc, i), dt);
+}
+}  // namespace
+
+static float tait_B(float rho0, float c0, float gamma) { return rho0 * c0 * c0 / gamma; }
+
+int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
+                float gamma, cudaStream_t st) {
+    const int n = c->sph.n;
+    if (n <= 0) return SPHDEM_OK;
+    DensArgs a;
+    a.gs = make_geo(c->grid_sph);
+    a.gb = make_geo(c->grid_bnd);
+    if (c->bnd.n <= 0) a.gb.ncl = 0;
+    a.f_posm = (const float4*)c->work.f_posm;
+    a.f_vprev = c->work.f_vprev;
+    a.b_posm = (const float4*)c->work.b_posm;
+    a.b_vprev = c->work.b_vprev;
+    a.flt = c->sph.flt;
+    a.rho = c->sph.rho;
+    a.pres = c->sph.pres;
+    a.f_rp = (float4*)c->work.f_rp;
+    a.f_posv = (float4*)c->work.f_posv;
+    a.n = n;
+    a.s2 = support * support;
+    a.rq = pad_radius(support);
+    a.kern = make_kern(h);
+    a.rho0 = rho0;
+    a.B = tait_B(rho0, c0, gamma);
+    a.gamma = gamma;
+    const int nb = blocks_for(n, 128);
+    if (flt && rho && pres)
+        k_density<true, true, true><<<nb, 128, 0, st>>>(a);
+    else if (!flt && rho && pres)
+        k_density<false, true, true><<<nb, 128, 0, st>>>(a);
+    else if (flt && !rho)
+        k_density<true, false, false><<<nb, 128, 0, st>>>(a);
+    else if (!flt && rho && !pres)
+        k_density<false, true, false><<<nb, 128, 0, st>>>(a);
+    else
+        k_density<true, true, false><<<nb, 128, 0, st>>>(a);
+    return launch_status("density");
+}
+
+int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, float rho0, float c0, float gamma,
+                     cudaStream_t st) {
+    const int n = c->bnd.n;
+    if (n <= 0) return SPHDEM_OK;
+    WallArgs a;
+    a.gs = make_geo(c->grid_sph);
+    if (c->sph.n <= 0) a.gs.ncl = 0;
+    a.gb = make_geo(c->grid_bnd);
+    a.f_posm = (const float4*)c->work.f_posm;
+    a.b_posm = (const float4*)c->work.b_posm;
+    a.b_self = c->work.b_self;
+    a.rho = c->bnd.rho;
+    a.pres = c->bnd.pres;
+    a.b_rp = (float4*)c->work.b_rp;
+    a.n = n;
+    a.s2 = support * support;
+    a.rq = pad_radius(support);
+    a.kern = make_kern(h);
+    a.rho0 = rho0;
+    a.B = tait_B(rho0, c0, gamma);
+    a.gamma = gamma;
+    if (pres)
+        k_density_wall<true><<<blocks_for(n, 128), 128, 0, st>>>(a);
+    else
+        k_density_wall<false><<<blocks_for(n, 128), 128, 0, st>>>(a);
+    return launch_status("density_wall");
+}
+
+int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st) {
+    const int n = c->sph.n;
+    if (n <= 0) return SPHDEM_OK;
+    ForceArgs a;
+    a.gs = make_geo(c->grid_sph);
+    a.gb = make_geo(c->grid_bnd);
+    if (c->bnd.n <= 0) a.gb.ncl = 0;
+    a.f_posm = (const float4*)c->work.f_posm;
+    a.f_vel = (const float4*)c->work.f_vel;
+    a.f_rp = (const float4*)c->work.f_rp;
+    a.b_posm = (const float4*)c->work.b_posm;
+    a.b_vel = (const float4*)c->work.b_vel;
+    a.b_rp = (const float4*)c->work.b_rp;
+    a.acc = c->sph.acc;
+    a.pgf = c->sph.pgf;
+    a.f_pgf = (float4*)c->work.f_pgf;
+    a.n = n;
+    a.s2 = support * support;
+    a.rq = pad_radius(support);
+    a.kern = make_kern(h);
+    a.two_mu = 2.0f * mu;
+    a.eps_h2 = 0.01f * h * h;
+    a.g = g;
+    const int nb = blocks_for(n, 128);
+    if (mode == 3)
+        k_force<3><<<nb, 128, 0, st>>>(a);
+    else if (mode == 2)
+        k_force<2><<<nb, 128, 0, st>>>(a);
+    else
+        k_force<1><<<nb, 128, 0, st>>>(a);
+    return launch_status("force");
+}
+
+int run_pres(const float* rho, float* pres, int n, float rho0, float c0, float gamma, cudaStream_t st) {
+    if (n <= 0) return SPHDEM_OK;
+    k_pres<<<blocks_for(n, 256), 256, 0, st>>>(rho, pres, n, rho0, tait_B(rho0, c0, gamma), gamma);
+    return launch_status("pres");
+}
+
+int run_step_sph(const sphdem_ctx_t* c, float dt, cudaStream_t st) {
+    const int n = c->sph.n;
+    if (n <= 0) return SPHDEM_OK;
+    k_step_sph<<<blocks_for(n, 256), 256, 0, st>>>(c->sph.pos, c->sph.vel, c->sph.acc, n, dt);
+    return launch_status("step_sph");
+}
+
+}  // namespace sd

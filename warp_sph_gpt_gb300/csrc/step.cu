@@ -1,0 +1,638 @@
+// step.cu -- the C ABI: step orchestration, CUDA-graph replay, single-kernel
+// entry points, verification digests and FP64 diagnostics.
+//
+// Step order follows source/Simulation.py:17-221:
+//   SPH:     [Shepard +] density + Tait (fluid) ; density + Tait (walls) ;
+//            force (+ -grad p when coupled)
+//   coupled: DEM-DEM and DEM-wall CSR rebuild with loads ; porosity ;
+//            fluid -> DEM exchange ; DEM -> fluid reaction + SPH integration ;
+//            DEM integration
+// The -grad p half of Kernel_prep_sphdem moves into the force loop: it reads
+// the same pressures, positions and neighbours, none of which the DEM contact
+// stage in between can change.
+#include <stdio.h>
+#include <string.h>
+
+#include <map>
+#include <mutex>
+
+#include "common.cuh"
+
+namespace sd {
+
+int build_grid(sphdem_grid_t* g, const float* pos, sphdem_ctl_t* ctl, cudaStream_t st);
+int gather_fluid(const sphdem_ctx_t* c, cudaStream_t st);
+int gather_wall(const sphdem_ctx_t* c, float support, float h, cudaStream_t st);
+int gather_wall_rho(const sphdem_ctx_t* c, cudaStream_t st);
+int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
+                float gamma, cudaStream_t st);
+int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, float rho0, float c0, float gamma,
+                     cudaStream_t st);
+int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st);
+int run_pres(const float* rho, float* pres, int n, float rho0, float c0, float gamma, cudaStream_t st);
+int run_step_sph(const sphdem_ctx_t* c, float dt, cudaStream_t st);
+int run_contacts(const sphdem_ctx_t* c, float radius_max, float bnd_radius_max, float g, float dt, int which,
+                 cudaStream_t st);
+int run_dem_aux(const sphdem_ctx_t* c, cudaStream_t st);
+int run_step_dem(const sphdem_ctx_t* c, float dt, cudaStream_t st);
+int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st);
+int run_interaction_dem(const sphdem_ctx_t* c, float mu, float eps_min, float eps_max, float dt, cudaStream_t st);
+int run_react(const sphdem_ctx_t* c, float support, float dt, bool integrate, cudaStream_t st);
+int run_drag_beta(const float* eps, const float* rho, const float* mu, const float* d, const float* speed, int n,
+                  float* out, cudaStream_t st);
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local char g_err[512] = "";
+
+void set_error(const char* where, cudaError_t e) {
+    snprintf(g_err, sizeof(g_err), "%s: %s (%d)", where, cudaGetErrorString(e), (int)e);
+}
+void set_error_msg(const char* msg) { snprintf(g_err, sizeof(g_err), "%s", msg); }
+int launch_status(const char* where) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+        set_error(where, e);
+        return SPHDEM_ERR_CUDA;
+    }
+    return SPHDEM_OK;
+}
+
+#define TRY(x)                   \
+    do {                         \
+        int rc_ = (x);           \
+        if (rc_) return rc_;     \
+    } while (0)
+
+namespace {
+
+bool shepard_due(const sphdem_params_t* p, int step) {
+    return step == 0 || (p->shepard_step > 0 && step % p->shepard_step == 0);  // source/Simulation.py:45
+}
+
+// SPH densities, pressures and forces (source/Simulation.py:53-91); mode 3
+// also forms -grad p for the coupling.  The pgf field is written only when
+// write_pgf; the acceleration arithmetic is the same either way.
+int sph_part(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool write_pgf, cudaStream_t st) {
+    if (shep) TRY(gather_wall_rho(c, st));
+    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st));
+    TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st));
+    sphdem_ctx_t cc = *c;
+    if (!write_pgf) cc.sph.pgf = nullptr;
+    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st);
+}
+
+int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integrate, cudaStream_t st) {
+    TRY(sph_part(c, p, shep, false, st));
+    if (integrate) TRY(run_step_sph(c, p->dt, st));
+    return SPHDEM_OK;
+}
+
+int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st) {
+    TRY(sph_part(c, p, shep, true, st));
+    TRY(run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, st));
+    TRY(run_dem_aux(c, st));
+    const float support = 2.0f * p->h_max;  // source/Simulation.py:208
+    TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, st));
+    TRY(run_interaction_dem(c, p->mu, p->porosity_min, p->porosity_max, p->dt, st));
+    TRY(run_react(c, support, p->dt, true, st));
+    return run_step_dem(c, p->dt, st);
+}
+
+// ---------------------------------------------------------------------------
+// sorted-copy refresh for the single-kernel entry points
+// ---------------------------------------------------------------------------
+__global__ void k_refresh_fluid(sphdem_sph_t P, const int* __restrict__ order, float4* posm, float4* vel,
+                                float* vprev, float4* rp, float4* posv, float4* pgf) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= P.n) return;
+    const int o = order[k];
+    const float m = P.m[o], rho = P.rho[o], pr = P.pres[o];
+    const float3 x = ld3(P.pos, o), v = ld3(P.vel, o), g = ld3(P.pgf, o);
+    posm[k] = make_float4(x.x, x.y, x.z, m);
+    vel[k] = make_float4(v.x, v.y, v.z, 0.f);
+    vprev[k] = m / rho;
+    rp[k] = make_float4(rho, pr, pr / (rho * rho), 1.0f / rho);
+    posv[k] = make_float4(x.x, x.y, x.z, m / rho);
+    pgf[k] = make_float4(g.x, g.y, g.z, rho);
+}
+
+__global__ void k_refresh_wall(sphdem_bnd_t B, const int* __restrict__ order, float4* posm, float4* vel, float* vprev,
+                               float4* rp) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= B.n) return;
+    const int o = order[k];
+    const float m = B.m[o], rho = B.rho[o], pr = B.pres[o];
+    const float3 x = ld3(B.pos, o), v = ld3(B.vel, o);
+    posm[k] = make_float4(x.x, x.y, x.z, m);
+    vel[k] = make_float4(v.x, v.y, v.z, 0.f);
+    vprev[k] = m / rho;
+    rp[k] = make_float4(rho, pr, pr / (rho * rho), 1.0f / rho);
+}
+
+// ---------------------------------------------------------------------------
+// CUDA-graph replay of run_forward's loop body
+// ---------------------------------------------------------------------------
+struct GraphEntry {
+    sphdem_ctx_t snap;
+    sphdem_params_t params;
+    int coupled = -1;
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    int kernels[2] = {0, 0};
+};
+std::mutex g_graph_mu;
+std::map<const sphdem_ctx_t*, GraphEntry> g_graphs;
+
+void drop_entry(GraphEntry& e) {
+    for (auto& x : e.exec)
+        if (x) {
+            cudaGraphExecDestroy(x);
+            x = nullptr;
+        }
+}
+
+int loop_body(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, int coupled, cudaStream_t st) {
+    TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
+    TRY(gather_fluid(c, st));
+    if (coupled) {
+        TRY(build_grid(&c->grid_dem, c->dem.pos, c->ctl, st));
+        return coupled_onestep(c, p, shep, st);
+    }
+    return sph_onestep(c, p, shep, true, st);
+}
+
+int capture(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, int coupled, GraphEntry& e) {
+    cudaError_t err = cudaStreamBeginCapture(e.cap, cudaStreamCaptureModeThreadLocal);
+    if (err != cudaSuccess) {
+        set_error("graph capture begin", err);
+        return SPHDEM_ERR_CUDA;
+    }
+    int rc = loop_body(c, p, shep, coupled, e.cap);
+    cudaGraph_t graph = nullptr;
+    err = cudaStreamEndCapture(e.cap, &graph);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (err != cudaSuccess) {
+        set_error("graph capture end", err);
+        return SPHDEM_ERR_CUDA;
+    }
+    size_t n_nodes = 0;
+    cudaGraphGetNodes(graph, nullptr, &n_nodes);
+    int n_kernels = 0;
+    if (n_nodes) {
+        cudaGraphNode_t* nodes = new cudaGraphNode_t[n_nodes];
+        cudaGraphGetNodes(graph, nodes, &n_nodes);
+        for (size_t i = 0; i < n_nodes; ++i) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++n_kernels;
+        }
+        delete[] nodes;
+    }
+    e.kernels[shep ? 1 : 0] = n_kernels;
+    err = cudaGraphInstantiate(&e.exec[shep ? 1 : 0], graph, 0);
+    cudaGraphDestroy(graph);
+    if (err != cudaSuccess) {
+        set_error("graph instantiate", err);
+        return SPHDEM_ERR_CUDA;
+    }
+    return SPHDEM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// verification digests
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+struct DigArgs {
+    Geo gsub, gnb;  // subject grid (instance lookup) and neighbour grid
+    const float* spos;
+    const float* npos;
+    int nsub;
+    int rel;
+    float s, s2, rq, t;  // radius, s*s, padded radius, sqrt bound of s
+    const float4* aux;  // per DEM (neighbour or subject)
+    const float* flt_s;
+    int32_t* count;
+    uint64_t* hash;
+};
+
+__global__ void k_digest(DigArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nsub) return;
+    const float3 p = ld3(a.spos, i);
+    const int inst = inst_of(a.gsub, i);
+    float rq = a.rq, t = a.t;
+    if (a.rel == SPHDEM_REL_DEM_SPH_2H || a.rel == SPHDEM_REL_DEM_DEM_2H) {
+        rq = pad_radius(a.aux[i].w);
+        t = a.aux[i].z;
+    }
+    int cnt = 0;
+    uint64_t hs = 0;
+    const Win w = window(a.gnb, p.x, p.y, p.z, rq);
+    for_each_range(a.gnb, w, inst, [&](int s, int e) {
+        for (int k = s; k < e; ++k) {
+            const int j = a.gnb.order[k];
+            const float3 q = ld3(a.npos, j);
+            const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+            bool in = false;
+            switch (a.rel) {
+                case SPHDEM_REL_SPH_SPH_SUPPORT:
+                case SPHDEM_REL_SPH_BND_SUPPORT:
+                case SPHDEM_REL_BND_SPH_SUPPORT:
+                case SPHDEM_REL_BND_BND_SUPPORT: in = r.d2 < a.s2; break;
+                case SPHDEM_REL_SPH_SPH_FORCE:
+                case SPHDEM_REL_SPH_BND_FORCE: in = r.d2 > kR2Min && r.d2 < a.s2; break;
+                case SPHDEM_REL_SPH_SPH_LEN:
+                case SPHDEM_REL_DEM_SPH_2H:
+                case SPHDEM_REL_DEM_DEM_2H: in = r.d2 < t; break;
+                case SPHDEM_REL_SPH_DEM_2H: in = r.d2 < a.aux[j].z; break;
+                case SPHDEM_REL_SPH_DEM_REACT: in = r.d2 < a.aux[j].z && a.flt_s[j] > 1.0e-12f; break;
+            }
+            if (in) {
+                ++cnt;
+                hs += mix64((uint64_t)j);
+            }
+        }
+    });
+    a.count[i] = cnt;
+    a.hash[i] = hs;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 diagnostics (no reference counterpart): one block, fixed order.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(1024) k_diag(sphdem_sph_t P, sphdem_dem_t D, float g, double* out) {
+    __shared__ double red[32][8];
+    double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    for (int i = threadIdx.x; i < P.n; i += blockDim.x) {
+        const double m = P.m[i], vx = P.vel[3 * i], vy = P.vel[3 * i + 1], vz = P.vel[3 * i + 2];
+        s[0] += m;
+        s[2] += m * vx;
+        s[3] += m * vy;
+        s[4] += m * vz;
+        s[5] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        s[7] += m * (double)g * (double)P.pos[3 * i + 2];
+    }
+    for (int a = threadIdx.x; a < D.n; a += blockDim.x) {
+        const double m = D.m[a], vx = D.vel[3 * a], vy = D.vel[3 * a + 1], vz = D.vel[3 * a + 2];
+        const double wx = D.omega[3 * a], wy = D.omega[3 * a + 1], wz = D.omega[3 * a + 2];
+        s[1] += m;
+        s[2] += m * vx;
+        s[3] += m * vy;
+        s[4] += m * vz;
+        s[5] += 0.5 * m * (vx * vx + vy * vy + vz * vz);
+        s[6] += 0.5 * (double)D.inertia[a] * (wx * wx + wy * wy + wz * wz);
+        s[7] += m * (double)g * (double)D.pos[3 * a + 2];
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int c = 0; c < 8; ++c) {
+        const double v = warp_sum(s[c]);
+        if (lane == 0) red[wid][c] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < 8) {
+        double t = 0.0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k][threadIdx.x];
+        out[threadIdx.x] = t;
+    }
+}
+
+__global__ void k_wendland(const float* r, int n, Kern k, float* w, float* dw) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    w[i] = kern_w(k, r[i]);
+    dw[i] = kern_dw(k, r[i]);
+}
+
+bool valid_ctx(const sphdem_ctx_t* c) {
+    if (!c || !c->ctl) {
+        set_error_msg("null context or control block");
+        return false;
+    }
+    return true;
+}
+
+}  // namespace
+}  // namespace sd
+
+using namespace sd;
+
+// ===========================================================================
+// extern "C"
+// ===========================================================================
+extern "C" {
+
+int sphdem_abi_version(void) { return SPHDEM_ABI_VERSION; }
+const char* sphdem_last_error(void) { return g_err; }
+
+// sizeof of the ABI structs, so a binding can check its mirror of them.
+int sphdem_struct_sizes(int64_t* out, int n) {
+    const int64_t s[] = {(int64_t)sizeof(sphdem_sph_t),   (int64_t)sizeof(sphdem_bnd_t),
+                         (int64_t)sizeof(sphdem_csr_t),   (int64_t)sizeof(sphdem_dem_t),
+                         (int64_t)sizeof(sphdem_dembnd_t), (int64_t)sizeof(sphdem_grid_t),
+                         (int64_t)sizeof(sphdem_ctl_t),   (int64_t)sizeof(sphdem_work_t),
+                         (int64_t)sizeof(sphdem_params_t), (int64_t)sizeof(sphdem_ctx_t)};
+    const int m = (int)(sizeof(s) / sizeof(s[0]));
+    for (int i = 0; i < n && i < m; ++i) out[i] = s[i];
+    return m;
+}
+
+int sphdem_grid_build(sphdem_ctx_t* c, int kind, const sphdem_params_t* p, sphdem_stream_t stream) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    switch (kind) {
+        case 0:
+            TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
+            return gather_fluid(c, st);
+        case 1:
+            TRY(build_grid(&c->grid_bnd, c->bnd.pos, c->ctl, st));
+            if (!p) {
+                set_error_msg("wall grid build needs params (support, h)");
+                return SPHDEM_ERR_INVALID;
+            }
+            return gather_wall(c, p->support, p->h, st);
+        case 2: return build_grid(&c->grid_dem, c->dem.pos, c->ctl, st);
+        case 3: return build_grid(&c->grid_dembnd, c->dembnd.pos, c->ctl, st);
+        default: set_error_msg("grid kind must be 0..3"); return SPHDEM_ERR_INVALID;
+    }
+}
+
+int sphdem_refresh_sorted(sphdem_ctx_t* c, sphdem_stream_t stream) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    const sphdem_work_t& w = c->work;
+    if (c->sph.n > 0)
+        k_refresh_fluid<<<blocks_for(c->sph.n, 256), 256, 0, st>>>(
+            c->sph, c->grid_sph.order, (float4*)w.f_posm, (float4*)w.f_vel, w.f_vprev, (float4*)w.f_rp,
+            (float4*)w.f_posv, (float4*)w.f_pgf);
+    if (c->bnd.n > 0)
+        k_refresh_wall<<<blocks_for(c->bnd.n, 256), 256, 0, st>>>(c->bnd, c->grid_bnd.order, (float4*)w.b_posm,
+                                                                  (float4*)w.b_vel, w.b_vprev, (float4*)w.b_rp);
+    TRY(launch_status("refresh_sorted"));
+    return run_dem_aux(c, st);
+}
+
+int sphdem_sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, int step, int integrate, sphdem_stream_t s) {
+    if (!valid_ctx(c) || !p) return SPHDEM_ERR_INVALID;
+    return sph_onestep(c, p, shepard_due(p, step), integrate != 0, as_stream(s));
+}
+
+int sphdem_sphdem_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, int step, sphdem_stream_t s) {
+    if (!valid_ctx(c) || !p) return SPHDEM_ERR_INVALID;
+    return coupled_onestep(c, p, shepard_due(p, step), as_stream(s));
+}
+
+int sphdem_run(sphdem_ctx_t* c, const sphdem_params_t* p, int first_step, int n_steps, int coupled,
+               sphdem_stream_t stream) {
+    if (!valid_ctx(c) || !p || n_steps < 0) return SPHDEM_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    GraphEntry& e = g_graphs[c];
+    if (e.coupled != coupled || memcmp(&e.snap, c, sizeof(*c)) != 0 || memcmp(&e.params, p, sizeof(*p)) != 0) {
+        drop_entry(e);
+        e.snap = *c;
+        e.params = *p;
+        e.coupled = coupled;
+    }
+    if (!e.cap) {
+        cudaError_t err = cudaStreamCreateWithFlags(&e.cap, cudaStreamNonBlocking);
+        if (err != cudaSuccess) {
+            set_error("capture stream", err);
+            return SPHDEM_ERR_CUDA;
+        }
+    }
+    for (int k = 0; k < n_steps; ++k) {
+        const bool shep = shepard_due(p, first_step + k);
+        cudaGraphExec_t& x = e.exec[shep ? 1 : 0];
+        if (!x) TRY(capture(c, p, shep, coupled, e));
+        cudaError_t err = cudaGraphLaunch(x, st);
+        if (err != cudaSuccess) {
+            set_error("graph launch", err);
+            return SPHDEM_ERR_CUDA;
+        }
+    }
+    return SPHDEM_OK;
+}
+
+// Blocking helper: one loop body of run_forward (moving-grid rebuild + one
+// step) with a CUDA event between phases on the launch stream; fills ms[k]
+// with the duration of phase k (SPHDEM_PHASE_* order) and synchronises.
+int sphdem_profile_step(sphdem_ctx_t* c, const sphdem_params_t* p, int step, int coupled, float* ms,
+                        sphdem_stream_t stream) {
+    if (!valid_ctx(c) || !p || !ms) return SPHDEM_ERR_INVALID;
+    cudaStream_t st = as_stream(stream);
+    cudaEvent_t ev[SPHDEM_PHASE_COUNT + 1];
+    for (auto& e : ev)
+        if (cudaEventCreate(&e) != cudaSuccess) return launch_status("profile events");
+    const bool shep = shepard_due(p, step);
+    int k = 0;
+    auto mark = [&]() { cudaEventRecord(ev[k++], st); };
+    int rc = SPHDEM_OK;
+    do {
+        mark();
+        if ((rc = build_grid(&c->grid_sph, c->sph.pos, c->ctl, st)) || (rc = gather_fluid(c, st))) break;
+        mark();
+        if (coupled && (rc = build_grid(&c->grid_dem, c->dem.pos, c->ctl, st))) break;
+        mark();
+        if (shep && (rc = gather_wall_rho(c, st))) break;
+        if ((rc = run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st))) break;
+        mark();
+        if ((rc = run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st))) break;
+        mark();
+        sphdem_ctx_t cc = *c;
+        if (!coupled) cc.sph.pgf = nullptr;
+        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st))) break;
+        mark();
+        if (coupled && (rc = run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, st))) break;
+        mark();
+        const float support = 2.0f * p->h_max;
+        if (coupled && ((rc = run_dem_aux(c, st)) ||
+                        (rc = run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, st))))
+            break;
+        mark();
+        if (coupled && (rc = run_interaction_dem(c, p->mu, p->porosity_min, p->porosity_max, p->dt, st))) break;
+        mark();
+        if (coupled ? (rc = run_react(c, support, p->dt, true, st)) : (rc = run_step_sph(c, p->dt, st))) break;
+        mark();
+        if (coupled && (rc = run_step_dem(c, p->dt, st))) break;
+        mark();
+    } while (0);
+    if (!rc) {
+        cudaError_t e = cudaEventSynchronize(ev[SPHDEM_PHASE_COUNT]);
+        if (e != cudaSuccess) {
+            set_error("profile sync", e);
+            rc = SPHDEM_ERR_CUDA;
+        }
+    }
+    for (int i = 0; !rc && i < SPHDEM_PHASE_COUNT; ++i) cudaEventElapsedTime(&ms[i], ev[i], ev[i + 1]);
+    for (auto& e : ev) cudaEventDestroy(e);
+    return rc;
+}
+
+// Kernel nodes in the captured loop-body graph of ctx (variant 1: Shepard
+// step, 0: other steps); -1 if that graph has not been captured.
+int sphdem_graph_kernels(sphdem_ctx_t* c, int variant) {
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    auto it = g_graphs.find(c);
+    if (it == g_graphs.end() || !it->second.exec[variant ? 1 : 0]) return -1;
+    return it->second.kernels[variant ? 1 : 0];
+}
+
+int sphdem_release(sphdem_ctx_t* c) {
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    auto it = g_graphs.find(c);
+    if (it == g_graphs.end()) return SPHDEM_OK;
+    drop_entry(it->second);
+    if (it->second.cap) cudaStreamDestroy(it->second.cap);
+    g_graphs.erase(it);
+    return SPHDEM_OK;
+}
+
+int sphdem_shepard_sph(sphdem_ctx_t* c, float support, float h, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_density(c, support, h, true, false, false, 1.f, 1.f, 1.f, as_stream(s));
+}
+int sphdem_density_sph(sphdem_ctx_t* c, float support, float h, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_density(c, support, h, false, true, false, 1.f, 1.f, 1.f, as_stream(s));
+}
+int sphdem_density_bnd(sphdem_ctx_t* c, float support, float h, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_density_wall(c, support, h, false, 1.f, 1.f, 1.f, as_stream(s));
+}
+int sphdem_pres_sph(sphdem_ctx_t* c, float rho0, float c0, float gamma, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_pres(c->sph.rho, c->sph.pres, c->sph.n, rho0, c0, gamma, as_stream(s));
+}
+int sphdem_pres_bnd(sphdem_ctx_t* c, float rho0, float c0, float gamma, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_pres(c->bnd.rho, c->bnd.pres, c->bnd.n, rho0, c0, gamma, as_stream(s));
+}
+int sphdem_force_sph(sphdem_ctx_t* c, float support, float h, float mu, float g, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_force(c, support, h, mu, g, 1, as_stream(s));
+}
+int sphdem_step_sph(sphdem_ctx_t* c, float dt, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_step_sph(c, dt, as_stream(s));
+}
+int sphdem_force_dem(sphdem_ctx_t* c, float radius_max, float g, float dt, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_contacts(c, radius_max, 0.0f, g, dt, 1, as_stream(s));
+}
+int sphdem_bc_dem(sphdem_ctx_t* c, float radius_max, float dt, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_contacts(c, 0.0f, radius_max, 0.0f, dt, 2, as_stream(s));
+}
+int sphdem_step_dem(sphdem_ctx_t* c, float dt, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    return run_step_dem(c, dt, as_stream(s));
+}
+int sphdem_prep_sphdem(sphdem_ctx_t* c, float support, float h, float sph_support, float sph_h, float eps_min,
+                       float eps_max, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    cudaStream_t st = as_stream(s);
+    TRY(run_dem_aux(c, st));
+    TRY(run_porosity(c, support, h, eps_min, eps_max, st));
+    sphdem_ctx_t cc = *c;  // -grad p only (mode 2)
+    return run_force(&cc, sph_support, sph_h, 0.0f, 0.0f, 2, st);
+}
+int sphdem_interaction_dem(sphdem_ctx_t* c, float mu, float eps_min, float eps_max, float dt, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    cudaStream_t st = as_stream(s);
+    TRY(run_dem_aux(c, st));
+    return run_interaction_dem(c, mu, eps_min, eps_max, dt, st);
+}
+int sphdem_interaction_sph(sphdem_ctx_t* c, float support, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    cudaStream_t st = as_stream(s);
+    TRY(run_dem_aux(c, st));
+    return run_react(c, support, 0.0f, false, st);
+}
+
+int sphdem_wendland(const float* r, int32_t n, float h, float* w, float* dw, sphdem_stream_t s) {
+    if (n <= 0) return SPHDEM_OK;
+    k_wendland<<<blocks_for(n, 256), 256, 0, as_stream(s)>>>(r, n, make_kern(h), w, dw);
+    return launch_status("wendland");
+}
+
+int sphdem_drag_beta(const float* eps, const float* rho, const float* mu, const float* d, const float* speed,
+                     int32_t n, float* out, sphdem_stream_t s) {
+    return run_drag_beta(eps, rho, mu, d, speed, n, out, as_stream(s));
+}
+
+int sphdem_neighbour_digest(sphdem_ctx_t* c, int rel, float radius, int32_t* count, uint64_t* hash,
+                            sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    if (rel < 0 || rel >= SPHDEM_REL_COUNT) {
+        set_error_msg("unknown neighbour relation");
+        return SPHDEM_ERR_INVALID;
+    }
+    cudaStream_t st = as_stream(s);
+    TRY(run_dem_aux(c, st));
+    DigArgs a;
+    a.rel = rel;
+    a.s = radius;
+    a.s2 = radius * radius;
+    a.rq = pad_radius(radius);
+    a.t = sqrt_lt_bound(radius);
+    a.aux = (const float4*)c->work.dem_aux;
+    a.flt_s = c->dem.flt_s;
+    a.count = count;
+    a.hash = hash;
+    switch (rel) {
+        case SPHDEM_REL_BND_SPH_SUPPORT:
+        case SPHDEM_REL_BND_BND_SUPPORT:
+            a.gsub = make_geo(c->grid_bnd);
+            a.spos = c->bnd.pos;
+            a.nsub = c->bnd.n;
+            break;
+        case SPHDEM_REL_DEM_SPH_2H:
+        case SPHDEM_REL_DEM_DEM_2H:
+            a.gsub = make_geo(c->grid_dem);
+            a.spos = c->dem.pos;
+            a.nsub = c->dem.n;
+            break;
+        default:
+            a.gsub = make_geo(c->grid_sph);
+            a.spos = c->sph.pos;
+            a.nsub = c->sph.n;
+    }
+    switch (rel) {
+        case SPHDEM_REL_SPH_BND_SUPPORT:
+        case SPHDEM_REL_BND_BND_SUPPORT:
+        case SPHDEM_REL_SPH_BND_FORCE:
+            a.gnb = make_geo(c->grid_bnd);
+            a.npos = c->bnd.pos;
+            break;
+        case SPHDEM_REL_SPH_DEM_2H:
+        case SPHDEM_REL_DEM_DEM_2H:
+        case SPHDEM_REL_SPH_DEM_REACT:
+            a.gnb = make_geo(c->grid_dem);
+            a.npos = c->dem.pos;
+            break;
+        default:
+            a.gnb = make_geo(c->grid_sph);
+            a.npos = c->sph.pos;
+    }
+    if (a.nsub <= 0) return SPHDEM_OK;
+    k_digest<<<blocks_for(a.nsub, 128), 128, 0, st>>>(a);
+    return launch_status("digest");
+}
+
+int sphdem_diagnostics(sphdem_ctx_t* c, float g, double* out, sphdem_stream_t s) {
+    if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
+    k_diag<<<1, 1024, 0, as_stream(s)>>>(c->sph, c->dem, g, out);
+    return launch_status("diagnostics");
+}
+
+}  // extern "C"

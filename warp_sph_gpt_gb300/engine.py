@@ -1,0 +1,245 @@
+"""Execution context: binds particle structs and grids to libsphdem.
+
+A ``StepContext`` owns the sorted working copies, the scan scratch of the grids
+and the ctypes ``sphdem_ctx_t`` that points at every tensor; it is cached per
+(structs, grids) combination on the fluid (or DEM) struct.  Every call
+enqueues work on torch's current CUDA stream; nothing here synchronises the
+host except the explicit status checks and the exact-length CSR views.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import weakref
+
+import torch
+
+from . import _lib
+from .grid import HashGrid, empty_grid
+from .struct import BNDptl, DEMBNDptl, DEMptl, SPHptl
+
+KIND_SPH, KIND_BND, KIND_DEM, KIND_DEMBND = 0, 1, 2, 3
+
+
+def _require_cuda(t: torch.Tensor, name: str) -> None:
+    if not t.is_cuda:
+        raise RuntimeError(f"{name} must be a CUDA tensor: the GB300 step has no CPU path")
+    if t.dtype not in (torch.float32, torch.int32, torch.float64) or not t.is_contiguous():
+        raise RuntimeError(f"{name} must be a contiguous float32/int32 tensor")
+
+
+class StepContext:
+    def __init__(self, sph, bnd, dem, dembnd, grids, device):
+        self.device = torch.device(device)
+        self.lib = _lib.load()
+        self.sets = [sph if sph is not None else SPHptl(0, self.device),
+                     bnd if bnd is not None else BNDptl(0, self.device),
+                     dem if dem is not None else DEMptl(0, self.device),
+                     dembnd if dembnd is not None else DEMBNDptl(0, self.device)]
+        self.has = [x is not None for x in (sph, bnd, dem, dembnd)]
+        self.grids = [g if g is not None else empty_grid() for g in grids]
+        self.ctl = self.sets[2]._ctl if dem is not None else torch.zeros(16, dtype=torch.int32,
+                                                                          device=self.device)
+        self.ctx = _lib.CtxT()
+        self.params = _lib.ParamsT()
+        self.box = None
+        self.wall_key = None
+        self.built = [False] * 4
+        self._sig = None
+        self._status_host = torch.zeros(16, dtype=torch.int32, pin_memory=True)
+        self._status_event = None
+        self._alloc_work()
+        addr = C.addressof(self.ctx)
+        weakref.finalize(self, _release, self.lib, addr)
+
+    # -- buffers ---------------------------------------------------------------
+    def _alloc_work(self) -> None:
+        ns, nb, nd = self.sets[0].n, self.sets[1].n, self.sets[2].n
+        f = dict(dtype=torch.float32, device=self.device)
+        i = dict(dtype=torch.int32, device=self.device)
+        self.work = dict(
+            f_posm=torch.zeros((ns, 4), **f), f_vel=torch.zeros((ns, 4), **f), f_rp=torch.zeros((ns, 4), **f),
+            f_vprev=torch.zeros(ns, **f), f_posv=torch.zeros((ns, 4), **f), f_pgf=torch.zeros((ns, 4), **f),
+            near_list=torch.zeros(ns, **i), b_posm=torch.zeros((nb, 4), **f), b_vel=torch.zeros((nb, 4), **f),
+            b_rp=torch.zeros((nb, 4), **f), b_vprev=torch.zeros(nb, **f), b_self=torch.zeros(nb, **f),
+            dem_count=torch.zeros(2 * (nd + 1), **i), dem_aux=torch.zeros((nd, 4), **f))
+
+    def _domain(self):
+        """Union bounding box of all particle sets (one host sync, once)."""
+        if self.box is None:
+            los, his = [], []
+            for s in self.sets:
+                if s.n > 0:
+                    mn, mx = torch.aminmax(s.pos, dim=0)
+                    los.append(mn)
+                    his.append(mx)
+            if not los:
+                lo = [0.0, 0.0, 0.0]
+                hi = [1.0, 1.0, 1.0]
+            else:
+                lo = torch.stack(los).amin(0).tolist()
+                hi = torch.stack(his).amax(0).tolist()
+            # open top: leave room above for splashes (points beyond still bin correctly)
+            hi[2] = hi[2] + 0.5 * max(hi[2] - lo[2], 1e-6)
+            self.box = (lo, hi)
+        return self.box
+
+    # -- ctypes structure --------------------------------------------------------
+    def _signature(self):
+        sig = []
+        for s in self.sets:
+            for name in s.field_names():
+                if name.startswith(("contact_", "tang_")):
+                    continue
+                sig.append(getattr(s, name).data_ptr())
+        return tuple(sig)
+
+    def _fill(self) -> None:
+        sig = self._signature()
+        if sig == self._sig:
+            return
+        sph, bnd, dem, dembnd = self.sets
+        P = self.ctx.sph
+        for name in SPHptl._fields:
+            t = getattr(sph, name[0])
+            if sph.n:
+                _require_cuda(t, f"SPHptl.{name[0]}")
+            setattr(P, name[0], _lib.fptr(t))
+        P.n = sph.n
+        B = self.ctx.bnd
+        for name, _ in BNDptl._fields:
+            t = getattr(bnd, name)
+            if bnd.n:
+                _require_cuda(t, f"BNDptl.{name}")
+            setattr(B, name, _lib.fptr(t))
+        B.n = bnd.n
+        D = self.ctx.dem
+        for name, _ in DEMptl._fields:
+            t = getattr(dem, name)
+            if dem.n:
+                _require_cuda(t, f"DEMptl.{name}")
+            setattr(D, name, _lib.fptr(t))
+        for kind, arr in (("dem", D.csr_dem), ("bnd", D.csr_bnd)):
+            for k, side in enumerate(dem._kinds[kind].sides):
+                arr[k].offset = _lib.iptr(side.offset)
+                arr[k].id = _lib.iptr(side.id)
+                arr[k].tang = _lib.fptr(side.tang)
+                arr[k].tang64 = _lib.dptr(side.tang64)
+                arr[k].capacity = side.capacity
+        D.n = dem.n
+        W = self.ctx.dembnd
+        for name, _ in DEMBNDptl._fields:
+            t = getattr(dembnd, name)
+            if dembnd.n:
+                _require_cuda(t, f"DEMBNDptl.{name}")
+            setattr(W, name, _lib.fptr(t))
+        W.n = dembnd.n
+        w = self.ctx.work
+        for name, t in self.work.items():
+            setattr(w, name, _lib.iptr(t) if t.dtype == torch.int32 else _lib.fptr(t))
+        self.ctx.ctl = self.ctl.data_ptr()
+        self._sig = sig
+
+    def _fill_grids(self) -> None:
+        lo, hi = self._domain()
+        for k, (g, s) in enumerate(zip(self.grids, self.sets)):
+            g.ensure_geometry(lo, hi, s.n, self.device)
+            g.fill(getattr(self.ctx, ("grid_sph", "grid_bnd", "grid_dem", "grid_dembnd")[k]), s.n)
+
+    def set_params(self, solv, scales=None) -> None:
+        p = self.params
+        p.h = solv.h
+        p.support = solv.support
+        p.rho0 = solv.rho0
+        p.c0 = solv.c0
+        p.gamma = solv.gamma
+        p.mu = solv.mu
+        p.g = solv.g
+        p.dt = solv.dt
+        p.shepard_step = int(solv.shepard_step)
+        p.porosity_min = getattr(solv, "dem_porosity_min", 0.05)
+        p.porosity_max = getattr(solv, "dem_porosity_max", 1.0)
+        if scales is not None:
+            p.radius_max, p.boundary_radius_max, p.h_max, p.h_uniform = (float(x) for x in scales)
+
+    @property
+    def stream(self):
+        return C.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    # -- grids -------------------------------------------------------------------
+    def prepare(self, rebuild_moving=True, wall_key=None) -> None:
+        """Pointers, grid geometry, and device builds of stale grids.
+        wall_key = (support, h) of the wall self-density cache."""
+        self._fill()
+        self._fill_grids()
+        sph, bnd, dem, dembnd = self.sets
+        st = self.stream
+        for kind in (KIND_BND, KIND_DEMBND, KIND_SPH, KIND_DEM):
+            g = self.grids[kind]
+            s = self.sets[kind]
+            if self.has[kind] and g.points is not None and g.points.data_ptr() != s.pos.data_ptr() and s.n:
+                raise ValueError("a grid must be built on the positions of its particle struct")
+            moving = kind in (KIND_SPH, KIND_DEM)
+            need = not self.built[kind] or g.dirty or (moving and rebuild_moving)
+            if kind == KIND_BND and wall_key is not None and wall_key != self.wall_key:
+                need = True
+            if not need:
+                continue
+            params = self.params
+            if kind == KIND_BND and wall_key is not None:
+                params = _lib.ParamsT()
+                C.memmove(C.byref(params), C.byref(self.params), C.sizeof(params))
+                params.support, params.h = wall_key
+                self.wall_key = wall_key
+            _lib.check(self.lib.sphdem_grid_build(C.byref(self.ctx), kind, C.byref(params), st),
+                       f"grid build (kind {kind})")
+            g.dirty = False
+            self.built[kind] = True
+
+    def refresh(self) -> None:
+        _lib.check(self.lib.sphdem_refresh_sorted(C.byref(self.ctx), self.stream), "refresh sorted copies")
+
+    # -- status ------------------------------------------------------------------
+    def poll_status(self) -> None:
+        """Raise for device flags of an earlier step if its copy has landed."""
+        ev = self._status_event
+        if ev is not None and ev.query():
+            self._raise_for(int(self._status_host[3]))
+
+    def post_status(self) -> None:
+        self._status_host.copy_(self.ctl, non_blocking=True)
+        if self._status_event is None:
+            self._status_event = torch.cuda.Event()
+        self._status_event.record()
+
+    def check_status(self) -> None:
+        """Blocking check of the device status bits."""
+        self._raise_for(int(self.ctl[3].item()))
+
+    def _raise_for(self, flags: int) -> None:
+        if flags & (_lib.FLAG_CSR_DEM_OVERFLOW | _lib.FLAG_CSR_BND_OVERFLOW):
+            self.ctl[3] = 0
+            raise OverflowError("directed contact count exceeded the CSR capacity "
+                                f"(status 0x{flags:x}); allocate DEMptl with a larger capacity")
+        if flags & _lib.FLAG_NONFINITE:
+            self.ctl[3] = 0
+            raise FloatingPointError("non-finite particle position met while binning")
+
+
+def _release(lib, addr):
+    try:
+        lib.sphdem_release(C.c_void_p(addr))
+    except Exception:
+        pass
+
+
+def context_for(sph=None, bnd=None, dem=None, dembnd=None, grids=(None, None, None, None)) -> StepContext:
+    """Cached context for this combination of structs and grids."""
+    grids = tuple(HashGrid.from_id(g) if g is not None else None for g in grids)
+    owner = next(x for x in (sph, dem, bnd, dembnd) if x is not None)
+    key = tuple(id(x) if x is not None else 0 for x in (sph, bnd, dem, dembnd) + grids)
+    cache = owner.__dict__.setdefault("_sphdem_contexts", {})
+    ctx = cache.get(key)
+    if ctx is None:
+        ctx = StepContext(sph, bnd, dem, dembnd, grids, owner.pos.device)
+        cache[key] = ctx
+    return ctx
