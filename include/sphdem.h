@@ -301,6 +301,20 @@ int sphdem_force_dem(sphdem_ctx_t* c, float radius_max, float g, float dt, sphde
 /* Same for the DEM-wall CSR (kernel/KERNEL_DEM_BC.py:10-84, source/Simulation.py:175-203). */
 int sphdem_bc_dem(sphdem_ctx_t* c, float radius_max, float dt, sphdem_stream_t s);
 int sphdem_step_dem(sphdem_ctx_t* c, float dt, sphdem_stream_t s);                      /* kernel/KERNEL_DEM_step.py:6-30 */
+
+/* Contact rebuild for callers that cannot allocate device memory (no
+ * counterpart in the reference): the same count -> scan -> fill -> swap as
+ * sphdem_force_dem (which & 1) and sphdem_bc_dem (which & 2), but the per-row
+ * count scratch (work.dem_count) is a fixed array inside the library instead
+ * of a caller buffer; the caller still passes every input and output through
+ * ctx.  Limit: at most SPHDEM_NOALLOC_MAX_DEM moving spheres, larger inputs
+ * return SPHDEM_ERR_INVALID.  Allocates nothing.  The first call on a device
+ * looks up the array's device address, so make that first call before any
+ * stream capture.  All calls share the one array per device: calls whose GPU
+ * work overlaps (different streams) race on it. */
+#define SPHDEM_NOALLOC_MAX_DEM 65536
+int sphdem_contacts_noalloc(sphdem_ctx_t* c, float radius_max, float bnd_radius_max, float g,
+                            float dt, int which, sphdem_stream_t s);
 int sphdem_prep_sphdem(sphdem_ctx_t* c, float support, float h, float sph_support,
                        float sph_h, float eps_min, float eps_max, sphdem_stream_t s);   /* kernel/KERNEL_SPHDEM_interaction.py:43-115 */
 int sphdem_interaction_dem(sphdem_ctx_t* c, float mu, float eps_min, float eps_max,

@@ -113,6 +113,7 @@ _SIGNATURES = {
     "sphdem_force_dem": ([C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "sphdem_bc_dem": ([C.c_void_p, C.c_float, C.c_float, C.c_void_p], C.c_int),
     "sphdem_step_dem": ([C.c_void_p, C.c_float, C.c_void_p], C.c_int),
+    "sphdem_contacts_noalloc": ([C.c_void_p] + [C.c_float] * 4 + [C.c_int, C.c_void_p], C.c_int),
     "sphdem_prep_sphdem": ([C.c_void_p] + [C.c_float] * 6 + [C.c_void_p], C.c_int),
     "sphdem_interaction_dem": ([C.c_void_p] + [C.c_float] * 4 + [C.c_void_p], C.c_int),
     "sphdem_interaction_sph": ([C.c_void_p, C.c_float, C.c_void_p], C.c_int),

@@ -309,3 +309,77 @@ int run_step_dem(const sphdem_ctx_t* c, float dt, cudaStream_t st) {
 }
 
 }  // namespace sd
+
+// ===========================================================================
+// Contact rebuild without caller-provided scratch.
+//
+// Some callers cannot allocate device memory: a host code whose GPU memory
+// belongs to another framework's pool and that can only lend this library the
+// particle and contact buffers it already owns, or a time loop that must not
+// allocate once it runs.  For them the per-row contact counts, the only
+// scratch the contact rebuild needs, live in the fixed array below instead of
+// a caller buffer.  Every GPU that loads this library holds the array (512 KB)
+// until the process exits.
+// ===========================================================================
+#include <mutex>
+
+namespace {
+static __device__ __align__(256) int g_contact_count_scratch[2 * (SPHDEM_NOALLOC_MAX_DEM + 1)];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+int* g_scratch_ptr[kMaxDevices] = {};
+
+// Device address of the array on the current device, looked up once per
+// device.  In host code the array's name stands for a host-side shadow, not a
+// device address, so it must never be passed to a kernel directly.
+int scratch_for_current_device(int** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        sd::set_error("contacts (no-alloc): cudaGetDevice", e);
+        return SPHDEM_ERR_CUDA;
+    }
+    if (dev < 0 || dev >= kMaxDevices) {
+        sd::set_error_msg("contacts (no-alloc): device index beyond the supported range");
+        return SPHDEM_ERR_INVALID;
+    }
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_ptr[dev]) {
+        int* p = nullptr;
+        e = cudaGetSymbolAddress((void**)&p, g_contact_count_scratch);
+        if (e != cudaSuccess || !p) {
+            sd::set_error("contacts (no-alloc): cudaGetSymbolAddress", e);
+            return SPHDEM_ERR_CUDA;
+        }
+        g_scratch_ptr[dev] = p;
+    }
+    *out = g_scratch_ptr[dev];
+    return SPHDEM_OK;
+}
+}  // namespace
+
+extern "C" int sphdem_contacts_noalloc(sphdem_ctx_t* c, float radius_max, float bnd_radius_max, float g, float dt,
+                                       int which, sphdem_stream_t s) {
+    if (!c || !c->ctl) {
+        sd::set_error_msg("contacts (no-alloc): null context or control block");
+        return SPHDEM_ERR_INVALID;
+    }
+    if (which < 1 || which > 3) {
+        sd::set_error_msg("contacts (no-alloc): which must be 1 (DEM-DEM), 2 (DEM-wall) or 3 (both)");
+        return SPHDEM_ERR_INVALID;
+    }
+    if (c->dem.n > SPHDEM_NOALLOC_MAX_DEM) {
+        sd::set_error_msg("contacts (no-alloc): more moving DEM spheres than SPHDEM_NOALLOC_MAX_DEM (65536); "
+                          "use sphdem_force_dem / sphdem_bc_dem with caller scratch");
+        return SPHDEM_ERR_INVALID;
+    }
+    int* scratch = nullptr;
+    int rc = scratch_for_current_device(&scratch);
+    if (rc) return rc;
+    // Every count entry the rebuild reads is written by its own count pass
+    // first, so nothing left in the array by an earlier call is ever used.
+    sphdem_ctx_t cc = *c;
+    cc.work.dem_count = scratch;
+    return sd::run_contacts(&cc, radius_max, bnd_radius_max, g, dt, which, sd::as_stream(s));
+}
