@@ -159,6 +159,24 @@ def profile_traffic(kernel: str, workload: str):
     return None
 
 
+def reduce_max(value: float, world: int, device=None) -> float:
+    """Max of a per-rank float over all ranks (the timing rule: the slowest
+    replica sets the job time).  Identity for world == 1."""
+    if world <= 1:
+        return float(value)
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_throughput(units_per_replica: int, steps: int, world: int, ms_max: float) -> float:
+    """Whole-job particle-steps/s of `world` replicas timed by the slowest."""
+    return world * units_per_replica * steps / (ms_max * 1e-3)
+
+
 def gpu_arm(args, rank, world, local_rank):
     import torch
     import torch.distributed as dist
@@ -173,6 +191,7 @@ def gpu_arm(args, rank, world, local_rank):
     gen, solv, (P, B, D, W), desc = make_case(args.workload, device)
     scales = dem_search_scales(D, W)
     grids = [HashGrid() for _ in range(4)]
+    grids[0].cell_factor = grids[1].cell_factor = args.cell_factor
     grids[0].build(P.pos, solv.support)
     grids[1].build(B.pos, solv.support)
     grids[2].build(D.pos, max(2.0 * scales[0], 2.0 * scales[2]))
@@ -207,11 +226,7 @@ def gpu_arm(args, rank, world, local_rank):
     k1 = ctx.lib.sphdem_graph_kernels(C.byref(ctx.ctx), 1)
     k0 = ctx.lib.sphdem_graph_kernels(C.byref(ctx.ctx), 0)
     launches = shep * max(k1, 0) + (args.steps - shep) * max(k0, 0)
-    ms_max = ms
-    if world > 1:
-        t = torch.tensor([ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms_max = float(t.item())
+    ms_max = reduce_max(ms, world, device)
     ctx.check_status()
 
     # per-phase device times (CUDA events between phases, same stream)
@@ -261,15 +276,11 @@ def gpu_arm(args, rank, world, local_rank):
     e1.record(stream)
     torch.cuda.synchronize()
     barrier()
-    e2e_ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([e2e_ms], device=device)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = reduce_max(e0.elapsed_time(e1), world, device)
 
     result = {
         "metric": "particle-steps/s",
-        "value": world * n_units * args.steps / (ms_max * 1e-3),
+        "value": job_throughput(n_units, args.steps, world, ms_max),
         "unit": "particle-steps/s",
         "n_gpus": world,
         "steps": args.steps,
@@ -282,9 +293,10 @@ def gpu_arm(args, rank, world, local_rank):
         "data": "synthetic (seeded generator rules of the reference's input_gen)",
         "config": {"workload": desc, "fluid": P.n, "wall": B.n, "dem": D.n, "dem_wall": W.n,
                    "particles_counted": "fluid + moving DEM", "parallelism": f"replicas x{world}",
+                   "cell_factor": args.cell_factor,
                    "l2": "state > 129 MB L2 (no flush)" if args.workload == "large800k"
                    else "state < L2 (resident between steps, as in a run)"},
-        "e2e": {"value": world * n_units * e2e_steps / (e2e_ms * 1e-3), "unit": "particle-steps/s",
+        "e2e": {"value": job_throughput(n_units, e2e_steps, world, e2e_ms), "unit": "particle-steps/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                 "api": "SPHDEM_OneStep per step, state copied from / to pinned host memory"},
         "roofline": {"bound": "hbm", "kernel_phase": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -395,6 +407,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cell-factor", type=float, default=1.0,
+                    help="fluid/wall cell width as a fraction of the SPH support")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 

@@ -50,6 +50,8 @@ extern "C" {
 #define SPHDEM_FLAG_NONFINITE         0x4  /* a binned position was NaN/Inf         */
 #define SPHDEM_FLAG_ROW_OVERFLOW      0x8  /* one contact row exceeded the per-row
                                               sort buffer (rows still complete)     */
+#define SPHDEM_FLAG_TIMEOUT          0x10  /* a bounded wait on a shared-memory copy
+                                              gave up; that kernel's results are void */
 
 /* Opaque CUDA stream handle (cudaStream_t); 0 is the legacy default stream. */
 typedef void* sphdem_stream_t;
@@ -235,6 +237,10 @@ int         sphdem_abi_version(void);
 const char* sphdem_last_error(void);
 /* int32 words of scan scratch a grid with ncell cells needs. */
 int64_t     sphdem_scan_scratch(int64_t ncell);
+/* sizeof of the ABI structs, in declaration order (sph, bnd, csr, dem,
+ * dembnd, grid, ctl, work, params, ctx), for bindings to check their mirrors;
+ * writes min(n, count) values and returns the count. */
+int         sphdem_struct_sizes(int64_t* out, int n);
 
 /* ---- neighbour grid ---------------------------------------------------
  * Replaces wp.HashGrid.build(points, radius) (called at main.py:66,73,85,87).

@@ -1,0 +1,92 @@
+"""C ABI surface and the replica aggregation of bench.py (no GPU).
+
+* libsphdem.so loads without a GPU, reports its ABI version and exports every
+  function declared in include/sphdem.h; the ctypes mirrors of the ABI structs
+  have the library's own sizes.
+* bench.py --gpus N runs N independent replicas (the step does not shard);
+  the job time is the max over ranks, checked here with two gloo ranks.
+"""
+import ctypes as C
+import os
+import re
+import socket
+import sys
+from pathlib import Path
+
+import pytest
+import torch
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from warp_sph_gpt_gb300 import build
+
+    build.build_cuda()
+    from warp_sph_gpt_gb300 import _lib
+
+    return _lib.load()
+
+
+def declared_functions():
+    text = (ROOT / "include" / "sphdem.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(sphdem_\w+)\s*\(", text, flags=re.M))
+
+
+def test_library_loads_and_exports_every_declared_symbol(lib):
+    from warp_sph_gpt_gb300 import _lib
+
+    names = declared_functions()
+    assert len(names) >= 30
+    for name in sorted(names):
+        assert hasattr(lib, name), f"{name} declared in include/sphdem.h but not exported"
+    assert set(_lib.EXPORTED) == names  # the binding covers exactly the declared surface
+    assert lib.sphdem_abi_version() == _lib.ABI_VERSION
+    _lib.check_layout(lib)  # raises on any size mismatch
+
+
+def test_invalid_calls_return_status_without_a_gpu(lib):
+    assert lib.sphdem_sph_onestep(None, None, 0, 1, None) == 2
+    assert b"null context" in lib.sphdem_last_error()
+    assert lib.sphdem_neighbour_digest(None, 3, 1.0, None, None, None) == 2
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank_main(rank, world, port, out):
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+
+    ms = [12.0, 20.0][rank]
+    ms_max = bench.reduce_max(ms, world)
+    out[rank] = bench.job_throughput(1000, 10, world, ms_max)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_replica_time_is_max_over_ranks_gloo():
+    world = 2
+    out = mp.get_context("spawn").Manager().dict()
+    mp.start_processes(_rank_main, args=(world, _free_port(), out), nprocs=world, start_method="spawn")
+    expected = world * 1000 * 10 / 20.0e-3  # the slower replica sets the time
+    assert out[0] == pytest.approx(expected) and out[1] == pytest.approx(expected)
+
+
+def test_single_rank_is_identity():
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    assert bench.reduce_max(7.5, 1) == 7.5
+    assert bench.job_throughput(100, 4, 1, 2.0) == pytest.approx(200000.0)

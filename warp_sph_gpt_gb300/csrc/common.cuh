@@ -33,6 +33,7 @@ struct Geo {
     int lo[3];
     int dim[3];
     float inv;
+    float cell;  // cell width (1/inv)
     int ncl;    // cells per instance
     int ninst;  // instances sharing the geometry
     const int* __restrict__ start;
@@ -47,6 +48,7 @@ inline Geo make_geo(const sphdem_grid_t& g) {
         G.dim[d] = g.dim[d];
     }
     G.inv = g.inv_cell;
+    G.cell = g.cell;
     G.ncl = g.ncell_local;
     G.ninst = g.ninst;
     G.start = g.cell_start;
@@ -95,6 +97,125 @@ __device__ __forceinline__ void for_each_range(const Geo& g, const Win& w, int i
             if (s < e) f(s, e);
         }
 }
+
+// Ball-trimmed enumeration: like for_each_range, but each (x, y) column only
+// contributes the z cells that a ball of radius rq around p can reach over
+// that column's square, and columns beyond rq are skipped.  A point binned in
+// column (cx, cy) lies within `margin` of that column's square (binning is
+// floor(x * inv)), so its horizontal distance to p is at least the square's
+// gap; if it is within rq of p its z lies within sqrt(rq^2 - gap^2) of p.z
+// and its z cell is enumerated.  Face columns extend to infinity (clamping).
+template <class F>
+__device__ __forceinline__ void for_each_range_ball(const Geo& g, float px, float py, float pz, float rq, int inst,
+                                                    F&& f) {
+    const Win w = window(g, px, py, pz, rq);
+    const float rq2 = rq * rq;
+    const float margin = 0.01f * g.cell;
+    const int base_i = inst * g.ncl;
+    for (int cx = w.x0; cx <= w.x1; ++cx) {
+        const float x0 = cx == 0 ? -INFINITY : (float)(g.lo[0] + cx) * g.cell;
+        const float x1 = cx == g.dim[0] - 1 ? INFINITY : (float)(g.lo[0] + cx + 1) * g.cell;
+        const float gx = fmaxf(0.0f, fmaxf(x0 - px, px - x1) - margin);
+        const float gx2 = gx * gx;
+        if (gx2 > rq2) continue;
+        for (int cy = w.y0; cy <= w.y1; ++cy) {
+            const float y0 = cy == 0 ? -INFINITY : (float)(g.lo[1] + cy) * g.cell;
+            const float y1 = cy == g.dim[1] - 1 ? INFINITY : (float)(g.lo[1] + cy + 1) * g.cell;
+            const float gy = fmaxf(0.0f, fmaxf(y0 - py, py - y1) - margin);
+            const float rem = rq2 - gx2 - gy * gy;
+            if (rem < 0.0f) continue;
+            const float zr = sqrtf(rem) + margin;
+            const int z0 = coord(pz - zr, g.inv, g.lo[2], g.dim[2]);
+            const int z1 = coord(pz + zr, g.inv, g.lo[2], g.dim[2]);
+            const int base = base_i + (cx * g.dim[1] + cy) * g.dim[2];
+            const int s = __ldg(g.start + base + z0);
+            const int e = __ldg(g.start + base + z1 + 1);
+            if (s < e) f(s, e);
+        }
+    }
+}
+
+// Slot range [s, e) of column (cx, cy) trimmed to the ball (see above); empty
+// if the column lies beyond rq.
+__device__ __forceinline__ void column_range_ball(const Geo& g, int cx, int cy, float px, float py, float pz,
+                                                  float rq, int inst, int& s, int& e) {
+    const float margin = 0.01f * g.cell;
+    const float x0 = cx == 0 ? -INFINITY : (float)(g.lo[0] + cx) * g.cell;
+    const float x1 = cx == g.dim[0] - 1 ? INFINITY : (float)(g.lo[0] + cx + 1) * g.cell;
+    const float y0 = cy == 0 ? -INFINITY : (float)(g.lo[1] + cy) * g.cell;
+    const float y1 = cy == g.dim[1] - 1 ? INFINITY : (float)(g.lo[1] + cy + 1) * g.cell;
+    const float gx = fmaxf(0.0f, fmaxf(x0 - px, px - x1) - margin);
+    const float gy = fmaxf(0.0f, fmaxf(y0 - py, py - y1) - margin);
+    const float rem = rq * rq - gx * gx - gy * gy;
+    s = e = 0;
+    if (rem < 0.0f) return;
+    const float zr = sqrtf(rem) + margin;
+    const int z0 = coord(pz - zr, g.inv, g.lo[2], g.dim[2]);
+    const int z1 = coord(pz + zr, g.inv, g.lo[2], g.dim[2]);
+    const int base = inst * g.ncl + (cx * g.dim[1] + cy) * g.dim[2];
+    s = __ldg(g.start + base + z0);
+    e = __ldg(g.start + base + z1 + 1);
+}
+
+// Warp-cooperative ball enumeration: the 32 lanes trim 32 columns at a time
+// (instead of every lane trimming every column), then f(s, e) is called
+// warp-uniformly for each non-empty range, in column order.
+template <class F>
+__device__ __forceinline__ void warp_ranges_ball(const Geo& g, float px, float py, float pz, float rq, int inst,
+                                                 F&& f) {
+    const int lane = threadIdx.x & 31;
+    const Win w = window(g, px, py, pz, rq);
+    const int ny = w.y1 - w.y0 + 1;
+    const int ncols = (w.x1 - w.x0 + 1) * ny;
+    for (int c0 = 0; c0 < ncols; c0 += 32) {
+        int s = 0, e = 0;
+        const int c = c0 + lane;
+        if (c < ncols) column_range_ball(g, w.x0 + c / ny, w.y0 + c % ny, px, py, pz, rq, inst, s, e);
+        unsigned mask = __ballot_sync(0xffffffffu, e > s);
+        while (mask) {
+            const int src = __ffs(mask) - 1;
+            mask &= mask - 1;
+            f(__shfl_sync(0xffffffffu, s, src), __shfl_sync(0xffffffffu, e, src));
+        }
+    }
+}
+
+// Block-cooperative version: the NT threads trim NT columns at a time into
+// shared memory, then f(s, e) is called block-uniformly per non-empty range.
+template <int NT, class F>
+__device__ __forceinline__ void block_ranges_ball(const Geo& g, float px, float py, float pz, float rq, int inst,
+                                                  int* s_sh, int* e_sh, F&& f) {
+    const Win w = window(g, px, py, pz, rq);
+    const int ny = w.y1 - w.y0 + 1;
+    const int ncols = (w.x1 - w.x0 + 1) * ny;
+    for (int c0 = 0; c0 < ncols; c0 += NT) {
+        int s = 0, e = 0;
+        const int c = c0 + (int)threadIdx.x;
+        if (c < ncols) column_range_ball(g, w.x0 + c / ny, w.y0 + c % ny, px, py, pz, rq, inst, s, e);
+        s_sh[threadIdx.x] = s;
+        e_sh[threadIdx.x] = e;
+        __syncthreads();
+        const int m = ncols - c0 < NT ? ncols - c0 : NT;
+        for (int k = 0; k < m; ++k)
+            if (e_sh[k] > s_sh[k]) f(s_sh[k], e_sh[k]);
+        __syncthreads();
+    }
+}
+
+// Membership d2 < t for a candidate, exactly as the FP32 predicate with every
+// operation rounded, but decided from the cheaper contracted dot product
+// whenever it is clear of the bound: fma-contracted and fully rounded dot
+// products differ by a few ulps, far inside the 2^-20 relative band, so only
+// candidates inside the band pay for the exact re-evaluation.
+__device__ __forceinline__ bool d2_below(float dx, float dy, float dz, float t_lo, float t_hi, float t, float& d2) {
+    d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+    if (d2 < t_lo) return true;
+    if (d2 >= t_hi) return false;
+    const float ex = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    return ex < t;
+}
+__host__ __device__ __forceinline__ float band_lo(float t) { return t * (1.0f - 9.5367431640625e-7f); }
+__host__ __device__ __forceinline__ float band_hi(float t) { return t * (1.0f + 9.5367431640625e-7f); }
 
 __device__ __forceinline__ int inst_of(const Geo& g, int point) {
     return (g.ninst > 1 && g.ncl > 0) ? __ldg(g.key + point) / g.ncl : 0;

@@ -15,7 +15,11 @@
 //   k_react           Kernel_interaction_sph (:190-226) fused with
 //                     Kernel_step_sph (kernel/KERNEL_step.py:6-22).
 // Sums use fixed lane/warp orders, so every result is deterministic.
+#include <stdlib.h>
+#include <string.h>
+
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace sd {
 
@@ -64,45 +68,68 @@ __device__ __forceinline__ float w_aux(const float4& aux, float dist) {
     return q < 2.0f ? aux.y * u2 * u2 * (1.0f + 2.0f * q) : 0.0f;
 }
 
-// Porosity pass 1: dry particles get clamp(1); the rest are listed.
-__global__ void k_near(CplArgs a) {
+// V_j u^4 (1 + 2q) of one candidate if it lies inside the ball (exact FP32
+// membership d2 < t2, every operation rounded), else 0.  Branch-free: warps
+// walk 32 different candidates, so a branch on membership would diverge.
+// The factor 21/(16 pi h^3) is applied by the caller once per sum.
+__device__ __forceinline__ float ball_weight(float px, float py, float pz, const float4& q, float t2, float inv_h) {
+    const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
+    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+    const float qq = d2 * rsqrtf(d2 + 1.0e-30f) * inv_h;
+    const float u = fmaf(-0.5f, qq, 1.0f);
+    const float u2 = u * u;
+    const float w = q.w * u2 * u2 * fmaf(2.0f, qq, 1.0f);
+    return d2 < t2 ? w : 0.0f;
+}
+
+// Porosity pass 1: dry particles get clamp(1); the rest are listed.  The list
+// keeps slot order inside each block of 256 slots (ordered block compaction),
+// so consecutive entries are neighbours in space.
+__global__ void __launch_bounds__(256) k_near(CplArgs a) {
+    __shared__ int warp_tot[8];
+    __shared__ int base;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.P.n) return;
-    const int o = a.gs.order[k];
-    const float4 p = a.f_posv[k];
-    const int inst = inst_of(a.gs, o);
     bool near = false;
-    if (a.D.n > 0) {
-        const Win w = window(a.gd, p.x, p.y, p.z, a.rq);
-        for_each_range(a.gd, w, inst, [&](int s, int e) {
-            for (int j = s; j < e && !near; ++j) {
-                const int b = a.gd.order[j];
-                const float3 pb = ld3(a.D.pos, b);
-                const D2 r = d2_exact(p.x, p.y, p.z, pb.x, pb.y, pb.z);
-                if (r.d2 < a.aux[b].z) near = true;  // len < 2 h_b, :87-88
-            }
-        });
+    int o = 0;
+    if (k < a.P.n) {
+        o = a.gs.order[k];
+        const float4 p = a.f_posv[k];
+        const int inst = inst_of(a.gs, o);
+        if (a.D.n > 0) {
+            const Win w = window(a.gd, p.x, p.y, p.z, a.rq);
+            for_each_range(a.gd, w, inst, [&](int s, int e) {
+                for (int j = s; j < e && !near; ++j) {
+                    const int b = a.gd.order[j];
+                    const float3 pb = ld3(a.D.pos, b);
+                    const D2 r = d2_exact(p.x, p.y, p.z, pb.x, pb.y, pb.z);
+                    if (r.d2 < a.aux[b].z) near = true;  // len < 2 h_b, :87-88
+                }
+            });
+        }
     }
+    int total;
+    const int ex = block_exclusive_scan(near ? 1 : 0, warp_tot, total);
+    if (threadIdx.x == 0) base = total ? atomicAdd(&a.ctl->n_near, total) : 0;
+    __syncthreads();
     if (near)
-        a.near_list[atomicAdd(&a.ctl->n_near, 1)] = k;
-    else
+        a.near_list[base + ex] = k;
+    else if (k < a.P.n)
         a.P.porosity[o] = fminf(fmaxf(1.0f, a.eps_min), a.eps_max);
 }
 
-// Warp-strided fluid sum sum_j V_j W(r_ij) over len(r_ij) < 2h (bound t2).
+// Warp-strided fluid sum  sum_j V_j W(r_ij, h)  over len(r_ij) < 2h, where
+// t2 is the exact sqrt bound of 2h and kaux = (1/h, 21/(16 pi h^3), ., .).
+// Membership is exact (d2_below); for members r < 2h, so the Wendland
+// cut-off test is not needed and 21/(16 pi h^3) is applied once at the end.
 __device__ __forceinline__ float warp_fluid_sum(const CplArgs& a, int inst, float px, float py, float pz, float rq,
                                                 float t2, const float4& kaux) {
     const int lane = threadIdx.x & 31;
     float acc = 0.0f;
-    const Win w = window(a.gs, px, py, pz, rq);
-    for_each_range(a.gs, w, inst, [&](int s, int e) {
-        for (int j = s + lane; j < e; j += 32) {
-            const float4 q = a.f_posv[j];
-            const D2 r = d2_exact(px, py, pz, q.x, q.y, q.z);
-            if (r.d2 < t2) acc += q.w * w_aux(kaux, fast_sqrt(r.d2));
-        }
+    warp_ranges_ball(a.gs, px, py, pz, rq, inst, [&](int s, int e) {
+#pragma unroll 4
+        for (int j = s + lane; j < e; j += 32) acc += ball_weight(px, py, pz, a.f_posv[j], t2, kaux.x);
     });
-    return warp_sum(acc);
+    return warp_sum(acc) * kaux.y;
 }
 
 // Porosity pass 2: one warp per listed particle.
@@ -138,24 +165,227 @@ __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
     }
 }
 
+// ---------------------------------------------------------------------------
+// Porosity pass 2 for a uniform DEM h: shared-memory staged.  A CTA of 8 warps
+// takes 32 consecutive listed particles (4 per warp; neighbours in space),
+// trims the columns of their common query window to the ball around their
+// bounding box, and streams the candidate ranges through two shared buffers:
+// each buffer is packed with as many ranges (or range pieces) as fit, each
+// piece one 1D TMA bulk copy (cp.async.bulk), all completing on the buffer's
+// mbarrier; the next buffer fills while the current one is consumed.  Every
+// staged candidate is tested against the warp's 4 particles.  The candidate in
+// slot j is always handled by lane j % 32, in slot order, so each particle's
+// sum does not depend on how particles were grouped or buffers packed.
+// ---------------------------------------------------------------------------
+constexpr int kTileWarps = 8;
+constexpr int kTileThreads = kTileWarps * 32;
+constexpr int kSubjPerWarp = 1;
+constexpr int kGroup = kTileWarps * kSubjPerWarp;
+constexpr int kBuf = 1280;          // float4 per staging buffer (20 KB)
+constexpr int kMaxPieces = 96;      // copies per buffer
+constexpr int kMaxCols = 512;       // trimmed columns per batch
+constexpr int kWaitPolls = 1 << 20;
+
+struct TileShared {
+    float4 buf[2][kBuf];
+    uint64_t bar[2];
+    int4 piece[2][kMaxPieces];  // slot, count, buffer offset
+    int npiece[2];
+    int rs[kMaxCols], re[kMaxCols];
+    float4 subj[kGroup];
+    int wtot[kTileWarps];
+};
+
+// Packs staging buffer b with the candidate ranges from cursor (r, o) on:
+// every thread walks the same packing (so all agree on the cursor), thread 0
+// records the pieces and issues one bulk copy per piece, all completing on
+// the buffer's barrier.  Returns the number of staged candidates (0: done).
+__device__ __forceinline__ int tile_fill(TileShared& sh, int b, int m, int& r, int& o, const float4* src, int tid) {
+    int used = 0, np = 0, rr = r, oo = o;
+    while (rr < m && used < kBuf && np < kMaxPieces) {
+        const int take = min(sh.re[rr] - oo, kBuf - used);
+        used += take;
+        oo += take;
+        if (oo >= sh.re[rr] && ++rr < m) oo = sh.rs[rr];
+        ++np;
+    }
+    if (used == 0) return 0;
+    if (tid == 0) {
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&sh.bar[b], (uint32_t)used * 16u);
+        int u2 = 0, r2 = r, o2 = o;
+        for (int q = 0; q < np; ++q) {
+            const int take = min(sh.re[r2] - o2, kBuf - u2);
+            sh.piece[b][q] = make_int4(o2, take, u2, 0);
+            tma_load_1d(&sh.buf[b][u2], src + o2, (uint32_t)take * 16u, &sh.bar[b]);
+            u2 += take;
+            o2 += take;
+            if (o2 >= sh.re[r2] && ++r2 < m) o2 = sh.rs[r2];
+        }
+        sh.npiece[b] = np;
+    }
+    r = rr;
+    o = oo;
+    return used;
+}
+
+__global__ void __launch_bounds__(kTileThreads, 3) k_porosity_tiles(CplArgs a) {
+    __shared__ TileShared sh;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        mbar_init(&sh.bar[0], 1);
+        mbar_init(&sh.bar[1], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    uint32_t ph0 = 0u, ph1 = 0u;  // phase parity of each buffer's barrier
+    const int n_near = a.ctl->n_near;
+    const float rq = a.rq, t2 = a.t_support;
+    const float inv_h = a.kern.inv_h;
+    const Geo& G = a.gs;
+    const float margin = 0.01f * G.cell;
+    for (int g = blockIdx.x; g * kGroup < n_near; g += gridDim.x) {
+        // this warp's particles (a missing one repeats the group's first)
+        float3 p[kSubjPerWarp];
+        int kk[kSubjPerWarp];
+        bool ok[kSubjPerWarp];
+#pragma unroll
+        for (int s = 0; s < kSubjPerWarp; ++s) {
+            const int idx = g * kGroup + warp * kSubjPerWarp + s;
+            ok[s] = idx < n_near;
+            kk[s] = a.near_list[ok[s] ? idx : g * kGroup];
+            const float4 ps = a.f_posv[kk[s]];
+            p[s] = make_float3(ps.x, ps.y, ps.z);
+        }
+        if (lane < kSubjPerWarp) sh.subj[warp * kSubjPerWarp + lane] = a.f_posv[kk[lane]];
+        __syncthreads();
+        float bx0 = INFINITY, bx1 = -INFINITY, by0 = INFINITY, by1 = -INFINITY, bz0 = INFINITY, bz1 = -INFINITY;
+        for (int w = 0; w < kGroup; ++w) {
+            const float4 q = sh.subj[w];
+            bx0 = fminf(bx0, q.x); bx1 = fmaxf(bx1, q.x);
+            by0 = fminf(by0, q.y); by1 = fmaxf(by1, q.y);
+            bz0 = fminf(bz0, q.z); bz1 = fmaxf(bz1, q.z);
+        }
+        const int inst = 0;  // single-instance grids only (see run_porosity)
+        const int x0 = coord(bx0 - rq, G.inv, G.lo[0], G.dim[0]), x1 = coord(bx1 + rq, G.inv, G.lo[0], G.dim[0]);
+        const int y0 = coord(by0 - rq, G.inv, G.lo[1], G.dim[1]), y1 = coord(by1 + rq, G.inv, G.lo[1], G.dim[1]);
+        const int ny = y1 - y0 + 1, ncols = (x1 - x0 + 1) * ny;
+        float acc[kSubjPerWarp];
+#pragma unroll
+        for (int s = 0; s < kSubjPerWarp; ++s) acc[s] = 0.0f;
+        for (int c0 = 0; c0 < ncols; c0 += kMaxCols) {
+            // trim kMaxCols columns (contiguous per thread), compact the
+            // non-empty ranges in column order
+            constexpr int per = kMaxCols / kTileThreads;
+            int ls[per], le[per], cnt = 0;
+#pragma unroll
+            for (int u = 0; u < per; ++u) {
+                const int c = c0 + tid * per + u;
+                ls[u] = le[u] = 0;
+                if (c >= ncols) continue;
+                const int cx = x0 + c / ny, cy = y0 + c % ny;
+                const float xa = cx == 0 ? -INFINITY : (float)(G.lo[0] + cx) * G.cell;
+                const float xb = cx == G.dim[0] - 1 ? INFINITY : (float)(G.lo[0] + cx + 1) * G.cell;
+                const float ya = cy == 0 ? -INFINITY : (float)(G.lo[1] + cy) * G.cell;
+                const float yb = cy == G.dim[1] - 1 ? INFINITY : (float)(G.lo[1] + cy + 1) * G.cell;
+                const float gx = fmaxf(0.0f, fmaxf(xa - bx1, bx0 - xb) - margin);
+                const float gy = fmaxf(0.0f, fmaxf(ya - by1, by0 - yb) - margin);
+                const float rem = rq * rq - gx * gx - gy * gy;
+                if (rem < 0.0f) continue;
+                const float zr = sqrtf(rem) + margin;
+                const int z0 = coord(bz0 - zr, G.inv, G.lo[2], G.dim[2]);
+                const int z1 = coord(bz1 + zr, G.inv, G.lo[2], G.dim[2]);
+                const int base = inst * G.ncl + (cx * G.dim[1] + cy) * G.dim[2];
+                ls[u] = __ldg(G.start + base + z0);
+                le[u] = __ldg(G.start + base + z1 + 1);
+                if (le[u] > ls[u]) ++cnt;
+            }
+            int m;
+            int off = block_exclusive_scan(cnt, sh.wtot, m);
+#pragma unroll
+            for (int u = 0; u < per; ++u)
+                if (le[u] > ls[u]) {
+                    sh.rs[off] = ls[u];
+                    sh.re[off] = le[u];
+                    ++off;
+                }
+            __syncthreads();
+            if (m == 0) continue;
+            // Pack buffers from the cursor (r, o) of the compacted ranges.
+            int r = 0, o = sh.rs[0];
+            int b = 0;
+            int cur = tile_fill(sh, 0, m, r, o, a.f_posv, tid);
+            while (cur > 0) {
+                const int nxt = tile_fill(sh, b ^ 1, m, r, o, a.f_posv, tid);
+                const uint32_t ph = b ? ph1 : ph0;
+                const bool landed = mbar_wait(&sh.bar[b], ph, kWaitPolls);
+                if (b) ph1 ^= 1u; else ph0 ^= 1u;
+                if (__syncthreads_or(!landed)) {
+                    // a copy did not land: report, let the copies in flight
+                    // finish (bounded) and leave with the whole CTA
+                    if (tid == 0) flag(a.ctl, SPHDEM_FLAG_TIMEOUT);
+                    mbar_wait(&sh.bar[b], ph, kWaitPolls);
+                    if (nxt > 0) mbar_wait(&sh.bar[b ^ 1], b ? ph0 : ph1, kWaitPolls);
+                    return;
+                }
+                const int np = sh.npiece[b];
+                for (int pc = 0; pc < np; ++pc) {
+                    const int4 pe = sh.piece[b][pc];
+                    const float4* B = &sh.buf[b][pe.z];
+#pragma unroll 4
+                    for (int i = (lane - pe.x) & 31; i < pe.y; i += 32) {
+                        const float4 q = B[i];
+#pragma unroll
+                        for (int s = 0; s < kSubjPerWarp; ++s) acc[s] += ball_weight(p[s].x, p[s].y, p[s].z, q, t2, inv_h);
+                    }
+                }
+                __syncthreads();  // buffer b is free again
+                b ^= 1;
+                cur = nxt;
+            }
+        }
+#pragma unroll
+        for (int s = 0; s < kSubjPerWarp; ++s) {
+            const float flt = warp_sum(acc[s]) * a.kern.cw;
+            if (!ok[s]) continue;
+            float solid = 0.0f;
+            const float3 ps = p[s];  // a scalar copy: capturing the array would force it to memory
+            const Win w = window(a.gd, ps.x, ps.y, ps.z, rq);
+            for_each_range(a.gd, w, inst, [&](int s0, int e0) {
+                for (int j = s0; j < e0; ++j) {
+                    const int bb = a.gd.order[j];
+                    const float3 pb = ld3(a.D.pos, bb);
+                    const D2 rr = d2_exact(ps.x, ps.y, ps.z, pb.x, pb.y, pb.z);
+                    const float4 ab = a.aux[bb];
+                    if (rr.d2 < ab.z) solid += a.D.volume[bb] * w_aux(ab, fast_sqrt(rr.d2)) / (flt + 1.0e-20f);
+                }
+            });
+            if (lane == 0) a.P.porosity[a.gs.order[kk[s]]] = fminf(fmaxf(1.0f - solid, a.eps_min), a.eps_max);
+        }
+        __syncthreads();
+    }
+}
+
 constexpr int kIdThreads = 256;
 
 // Kernel_interaction_dem: one CTA per DEM a.
 __global__ void __launch_bounds__(kIdThreads) k_interaction_dem(CplArgs a) {
     __shared__ float red[kIdThreads / 32][8];
+    __shared__ int s_sh[kIdThreads], e_sh[kIdThreads];
     const int am = blockIdx.x;
     const float3 pa = ld3(a.D.pos, am);
     const float4 aux = a.aux[am];  // 1/h, cw, bound(2h), 2h
     const int inst = inst_of(a.gd, am);
     float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // flt, rho_f, vel_f xyz, pgf xyz
     if (a.P.n > 0) {
-        const Win w = window(a.gs, pa.x, pa.y, pa.z, pad_radius(aux.w));
-        for_each_range(a.gs, w, inst, [&](int rs, int re) {
+        const float t_lo = band_lo(aux.z), t_hi = band_hi(aux.z);
+        block_ranges_ball<kIdThreads>(a.gs, pa.x, pa.y, pa.z, pad_radius(aux.w), inst, s_sh, e_sh,
+                                      [&](int rs, int re) {
             for (int j = rs + threadIdx.x; j < re; j += blockDim.x) {
                 const float4 q = a.f_posv[j];
-                const D2 r = d2_exact(pa.x, pa.y, pa.z, q.x, q.y, q.z);
-                if (r.d2 < aux.z) {  // len < 2 h_a, :157-158
-                    const float Vw = q.w * w_aux(aux, fast_sqrt(r.d2));
+                float d2;
+                if (d2_below(pa.x - q.x, pa.y - q.y, pa.z - q.z, t_lo, t_hi, aux.z, d2)) {  // len < 2 h_a, :157-158
+                    const float Vw = q.w * w_aux(aux, fast_sqrt(d2));
                     const float4 v = a.f_vel[j];
                     const float4 g = a.f_pgf[j];
                     s[0] += Vw;
@@ -296,10 +526,24 @@ int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, f
         int dev = 0, sms = 148;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        int blocks = sms * 8;
-        const int need = blocks_for(n, 8);
-        if (need < blocks) blocks = need;
-        k_porosity_near<<<blocks, 256, 0, st>>>(a);
+        // Two implementations of the uniform-h sum (same results, see the
+        // kernels); SPHDEM_POROSITY_KERNEL=staged selects the shared-memory
+        // staged one.  Grouped staging needs one instance per group.
+        static const bool staged = [] {
+            const char* v = getenv("SPHDEM_POROSITY_KERNEL");
+            return v && strcmp(v, "staged") == 0;
+        }();
+        if (staged && h > 0.0f && c->grid_sph.ninst <= 1) {
+            const int need = blocks_for(n, kGroup);
+            int blocks = sms * 4;  // resident CTAs of k_porosity_tiles per SM
+            if (need < blocks) blocks = need;
+            k_porosity_tiles<<<blocks, kTileThreads, 0, st>>>(a);
+        } else {
+            const int need = blocks_for(n, 8);
+            int blocks = sms * 8;
+            if (need < blocks) blocks = need;
+            k_porosity_near<<<blocks, 256, 0, st>>>(a);
+        }
     }
     return launch_status("porosity");
 }

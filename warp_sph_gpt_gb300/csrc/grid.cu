@@ -131,9 +131,8 @@ __global__ void k_wall_self(Geo gb, const float4* __restrict__ posm, int n, floa
     if (k >= n) return;
     float4 p = posm[k];
     int inst = inst_of(gb, gb.order[k]);
-    Win w = window(gb, p.x, p.y, p.z, rq);
     float acc = 0.0f;
-    for_each_range(gb, w, inst, [&](int s, int e) {
+    for_each_range_ball(gb, p.x, p.y, p.z, rq, inst, [&](int s, int e) {
         for (int j = s; j < e; ++j) {
             float4 q = posm[j];
             D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);

@@ -46,8 +46,7 @@ __global__ void __launch_bounds__(128) k_density(DensArgs a) {
     const float4 p = a.f_posm[k];
     const int inst = inst_of(a.gs, o);
     float rho_sum = 0.0f, flt_sum = 0.0f;
-    const Win ws = window(a.gs, p.x, p.y, p.z, a.rq);
-    for_each_range(a.gs, ws, inst, [&](int s, int e) {
+    for_each_range_ball(a.gs, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
         for (int j = s; j < e; ++j) {
             const float4 q = a.f_posm[j];
             const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
@@ -59,8 +58,7 @@ __global__ void __launch_bounds__(128) k_density(DensArgs a) {
         }
     });
     if (a.gb.ncl > 0) {
-        const Win wb = window(a.gb, p.x, p.y, p.z, a.rq);
-        for_each_range(a.gb, wb, inst, [&](int s, int e) {
+        for_each_range_ball(a.gb, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
             for (int j = s; j < e; ++j) {
                 const float4 q = a.b_posm[j];
                 const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
@@ -110,8 +108,7 @@ __global__ void __launch_bounds__(128) k_density_wall(WallArgs a) {
     const int inst = inst_of(a.gb, o);
     float rho_sum = 0.0f;
     if (a.gs.ncl > 0) {
-        const Win ws = window(a.gs, p.x, p.y, p.z, a.rq);
-        for_each_range(a.gs, ws, inst, [&](int s, int e) {
+        for_each_range_ball(a.gs, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
             for (int j = s; j < e; ++j) {
                 const float4 q = a.f_posm[j];
                 const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
@@ -184,8 +181,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a) {
     const float4 rpi = a.f_rp[k];
     const int inst = inst_of(a.gs, o);
     float3 acc = make_float3(0.f, 0.f, 0.f), pgf = make_float3(0.f, 0.f, 0.f);
-    const Win ws = window(a.gs, p.x, p.y, p.z, a.rq);
-    for_each_range(a.gs, ws, inst, [&](int s, int e) {
+    for_each_range_ball(a.gs, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
         for (int j = s; j < e; ++j) {
             const float4 q = a.f_posm[j];
             const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
@@ -194,8 +190,7 @@ __global__ void __launch_bounds__(128) k_force(ForceArgs a) {
         }
     });
     if (a.gb.ncl > 0) {
-        const Win wb = window(a.gb, p.x, p.y, p.z, a.rq);
-        for_each_range(a.gb, wb, inst, [&](int s, int e) {
+        for_each_range_ball(a.gb, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
             for (int j = s; j < e; ++j) {
                 const float4 q = a.b_posm[j];
                 const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);

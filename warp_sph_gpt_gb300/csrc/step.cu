@@ -237,8 +237,7 @@ __global__ void k_digest(DigArgs a) {
     }
     int cnt = 0;
     uint64_t hs = 0;
-    const Win w = window(a.gnb, p.x, p.y, p.z, rq);
-    for_each_range(a.gnb, w, inst, [&](int s, int e) {
+    for_each_range_ball(a.gnb, p.x, p.y, p.z, rq, inst, [&](int s, int e) {
         for (int k = s; k < e; ++k) {
             const int j = a.gnb.order[k];
             const float3 q = ld3(a.npos, j);

@@ -220,6 +220,9 @@ class StepContext:
             self.ctl[3] = 0
             raise OverflowError("directed contact count exceeded the CSR capacity "
                                 f"(status 0x{flags:x}); allocate DEMptl with a larger capacity")
+        if flags & _lib.FLAG_TIMEOUT:
+            self.ctl[3] = 0
+            raise RuntimeError("a bounded device-side wait timed out (status 0x%x); the step is void" % flags)
         if flags & _lib.FLAG_NONFINITE:
             self.ctl[3] = 0
             raise FloatingPointError("non-finite particle position met while binning")

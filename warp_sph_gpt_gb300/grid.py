@@ -48,6 +48,9 @@ class HashGrid:
         self.ninst = 1
         self.inst = None  # optional per-point instance ids (batched ensembles)
         self.buffers = None
+        # cell width = radius * cell_factor; neighbour sets do not depend on it
+        # (only the candidate count does), so it is a tuning parameter
+        self.cell_factor = 1.0
         self.id = next(_IDS)
         _REGISTRY[self.id] = self
 
@@ -75,7 +78,7 @@ class HashGrid:
         """Fix the cell box the first time (or after a radius change)."""
         if self.geometry is not None:
             return
-        cell = float(torch.tensor(self.radius, dtype=torch.float32).item())
+        cell = float(torch.tensor(self.radius * self.cell_factor, dtype=torch.float32).item())
         while True:
             inv = float(torch.tensor(1.0 / cell, dtype=torch.float32).item())
             lo, dim = [], []
