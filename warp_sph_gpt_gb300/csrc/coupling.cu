@@ -72,14 +72,15 @@ __device__ __forceinline__ float w_aux(const float4& aux, float dist) {
 // membership d2 < t2, every operation rounded), else 0.  Branch-free: warps
 // walk 32 different candidates, so a branch on membership would diverge.
 // The factor 21/(16 pi h^3) is applied by the caller once per sum.
-__device__ __forceinline__ float ball_weight(float px, float py, float pz, const float4& q, float t2, float inv_h) {
+__device__ __forceinline__ float ball_weight(float px, float py, float pz, const float4& q, float t2, float ih2) {
     const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
     const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-    const float qq = d2 * rsqrtf(d2 + 1.0e-30f) * inv_h;
+    const float x = fmaf(d2, ih2, 1.0e-30f);  // q^2 (guarded at 0)
+    const float qq = x * rsqrtf(x);           // q = r / h
     const float u = fmaf(-0.5f, qq, 1.0f);
     const float u2 = u * u;
-    const float w = q.w * u2 * u2 * fmaf(2.0f, qq, 1.0f);
-    return d2 < t2 ? w : 0.0f;
+    const float vu4 = d2 < t2 ? q.w * u2 * u2 : 0.0f;
+    return vu4 * fmaf(2.0f, qq, 1.0f);
 }
 
 // Porosity pass 1: dry particles get clamp(1); the rest are listed.  The list
@@ -124,10 +125,11 @@ __global__ void __launch_bounds__(256) k_near(CplArgs a) {
 __device__ __forceinline__ float warp_fluid_sum(const CplArgs& a, int inst, float px, float py, float pz, float rq,
                                                 float t2, const float4& kaux) {
     const int lane = threadIdx.x & 31;
+    const float ih2 = kaux.x * kaux.x;
     float acc = 0.0f;
     warp_ranges_ball(a.gs, px, py, pz, rq, inst, [&](int s, int e) {
 #pragma unroll 4
-        for (int j = s + lane; j < e; j += 32) acc += ball_weight(px, py, pz, a.f_posv[j], t2, kaux.x);
+        for (int j = s + lane; j < e; j += 32) acc += ball_weight(px, py, pz, a.f_posv[j], t2, ih2);
     });
     return warp_sum(acc) * kaux.y;
 }
@@ -241,7 +243,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_porosity_tiles(CplArgs a) {
     uint32_t ph0 = 0u, ph1 = 0u;  // phase parity of each buffer's barrier
     const int n_near = a.ctl->n_near;
     const float rq = a.rq, t2 = a.t_support;
-    const float inv_h = a.kern.inv_h;
+    const float ih2 = a.kern.inv_h * a.kern.inv_h;
     const Geo& G = a.gs;
     const float margin = 0.01f * G.cell;
     for (int g = blockIdx.x; g * kGroup < n_near; g += gridDim.x) {
@@ -336,7 +338,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_porosity_tiles(CplArgs a) {
                     for (int i = (lane - pe.x) & 31; i < pe.y; i += 32) {
                         const float4 q = B[i];
 #pragma unroll
-                        for (int s = 0; s < kSubjPerWarp; ++s) acc[s] += ball_weight(p[s].x, p[s].y, p[s].z, q, t2, inv_h);
+                        for (int s = 0; s < kSubjPerWarp; ++s) acc[s] += ball_weight(p[s].x, p[s].y, p[s].z, q, t2, ih2);
                     }
                 }
                 __syncthreads();  // buffer b is free again

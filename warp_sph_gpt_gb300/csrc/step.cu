@@ -89,12 +89,60 @@ int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integ
     return SPHDEM_OK;
 }
 
+// A side stream and two events per device for the concurrent DEM branch.
+struct Fork {
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+};
+std::mutex g_fork_mu;
+Fork g_fork[64];
+
+int fork_for_current_device(Fork** out) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return launch_status("fork device");
+    std::lock_guard<std::mutex> lock(g_fork_mu);
+    Fork& f = g_fork[dev];
+    if (!f.side) {
+        cudaError_t e = cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            set_error("fork stream", e);
+            return SPHDEM_ERR_CUDA;
+        }
+    }
+    *out = &f;
+    return SPHDEM_OK;
+}
+
+// The DEM contact rebuild reads only DEM and wall-sphere state, so it runs on
+// a side stream while the fluid density / force / porosity chain runs on the
+// main one (a fork/join of events; inside a graph capture this becomes two
+// parallel branches); the fluid -> DEM exchange waits for both.
 int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st) {
-    TRY(sph_part(c, p, shep, true, st));
-    TRY(run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, st));
     TRY(run_dem_aux(c, st));
+    Fork* f = nullptr;
+    TRY(fork_for_current_device(&f));
+    cudaError_t e = cudaEventRecord(f->fork, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(f->side, f->fork, 0);
+    if (e != cudaSuccess) {
+        set_error("fork", e);
+        return SPHDEM_ERR_CUDA;
+    }
+    TRY(run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, f->side));
+    e = cudaEventRecord(f->join, f->side);
+    if (e != cudaSuccess) {
+        set_error("join record", e);
+        return SPHDEM_ERR_CUDA;
+    }
+    TRY(sph_part(c, p, shep, true, st));
     const float support = 2.0f * p->h_max;  // source/Simulation.py:208
     TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, st));
+    e = cudaStreamWaitEvent(st, f->join, 0);
+    if (e != cudaSuccess) {
+        set_error("join", e);
+        return SPHDEM_ERR_CUDA;
+    }
     TRY(run_interaction_dem(c, p->mu, p->porosity_min, p->porosity_max, p->dt, st));
     TRY(run_react(c, support, p->dt, true, st));
     return run_step_dem(c, p->dt, st);
