@@ -5,7 +5,8 @@ Workload (default): the 800k-fluid variant of the large dam break -- tank
 fluid, 2,157,576 dummy wall particles), 2,000 DEM spheres R ~ U[0.01, 0.03]
 rejection-sampled above the water, 178,528 DEM wall spheres, dt = 2.5e-5 --
 generated from seeded rules (synthetic data).  ``--workload scaled`` runs the
-dx = 0.01 dam break (100,000 fluid, 160 DEM).
+dx = 0.01 dam break (100,000 fluid, 160 DEM); ``--workload batch64`` advances
+64 seeded dx = 0.02 dam breaks of different sizes as one batched state.
 
 A step is one loop body of run_forward: moving grids re-binned + one coupled
 SPHDEM step, replayed from CUDA graphs.  value = (fluid + DEM) particles x
@@ -66,8 +67,12 @@ def log(*a):
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
-def make_case(workload: str, device):
-    from warp_sph_gpt_gb300.generate import build_case, config_large, config_scaled, solver_config
+WORKLOADS = ("large800k", "scaled", "batch64")
+BATCH_MEMBERS = 64
+
+
+def _case_spec(workload: str):
+    from warp_sph_gpt_gb300.generate import config_large, config_scaled
 
     if workload == "large800k":
         gen, pos, rad = config_large(fluid_width=0.167, seed=0, n_dem=2000)
@@ -78,9 +83,39 @@ def make_case(workload: str, device):
         desc = "scaled dam break: tank 2x0.4x1 m, fluid 0.5x0.4x0.5 m at dx=0.01, 160 DEM R=0.025, dt=5e-5"
     else:
         raise SystemExit(f"unknown workload {workload}")
+    return gen, pos, rad, desc
+
+
+def make_case(workload: str, device):
+    """One case as host/device structs (the reference arm uses member 0 of a batch)."""
+    from warp_sph_gpt_gb300.generate import build_case, config_batch_member, solver_config
+
+    if workload == "batch64":
+        gen, pos, rad = config_batch_member(0)
+        desc = f"batch member 0 of {BATCH_MEMBERS}"
+    else:
+        gen, pos, rad, desc = _case_spec(workload)
     P, B, D, W = build_case(gen, pos, rad, device=device)
     solv = solver_config(gen)
     return gen, solv, (P, B, D, W), desc
+
+
+def make_runner(workload: str, device, cell_factor: float = 1.0):
+    """GPU state of a workload: a Case, or an Ensemble of 64 seeded dam breaks."""
+    from warp_sph_gpt_gb300.batch import Case, Ensemble
+    from warp_sph_gpt_gb300.generate import config_batch_member
+
+    if workload == "batch64":
+        members = [config_batch_member(i) for i in range(BATCH_MEMBERS)]
+        r = Ensemble(members, device=device, cell_factor=cell_factor)
+        r.gen = members[0][0]
+        r.desc = (f"ensemble of {BATCH_MEMBERS} dam breaks (tank 2x0.4x1 m, dx=0.02, fluid block "
+                  "U[0.3,0.7] x 0.4 x U[0.3,0.6] m, 0-40 DEM R=0.025, dt=1e-4), one batched step")
+    else:
+        gen, pos, rad, desc = _case_spec(workload)
+        r = Case(gen, pos, rad, device=device, cell_factor=cell_factor)
+        r.gen, r.desc = gen, desc
+    return r
 
 
 # ---------------------------------------------------------------------------
@@ -182,20 +217,30 @@ def gpu_arm(args, rank, world, local_rank):
     import torch.distributed as dist
     import ctypes as C
 
-    from warp_sph_gpt_gb300 import HashGrid, SPHDEM_OneStep, dem_search_scales, run_steps
+    from warp_sph_gpt_gb300 import SPHDEM_OneStep, dem_search_scales, run_steps
     from warp_sph_gpt_gb300 import _lib
     from warp_sph_gpt_gb300.engine import context_for
 
     torch.cuda.set_device(local_rank)
     device = torch.device("cuda", local_rank)
-    gen, solv, (P, B, D, W), desc = make_case(args.workload, device)
-    scales = dem_search_scales(D, W)
-    grids = [HashGrid() for _ in range(4)]
-    grids[0].cell_factor = grids[1].cell_factor = args.cell_factor
-    grids[0].build(P.pos, solv.support)
-    grids[1].build(B.pos, solv.support)
-    grids[2].build(D.pos, max(2.0 * scales[0], 2.0 * scales[2]))
-    grids[3].build(W.pos, max(2.0 * scales[1], solv.support))
+    tuning = {}
+    if args.autotune:
+        from warp_sph_gpt_gb300.autotune import autotune, case_key
+
+        probe = make_runner(args.workload, device)
+        key = case_key(probe.P, probe.B, probe.D, probe.W, probe.ninst)
+        del probe
+        tuning = autotune(lambda cf: make_runner(args.workload, device, cf), key,
+                          ninst=BATCH_MEMBERS if args.workload == "batch64" else 1, log=log)
+        args.cell_factor = tuning["cell_factor"]
+        log(f"[rank {rank}] autotuned: {tuning}")
+        torch.cuda.empty_cache()
+    runner = make_runner(args.workload, device, args.cell_factor)
+    if tuning:
+        runner.tune(tuning)
+    gen, solv, desc = runner.gen, runner.solv, runner.desc
+    P, B, D, W = runner.P, runner.B, runner.D, runner.W
+    scales, grids = runner.scales, runner.grids
     n_units = P.n + D.n
     log(f"[rank {rank}] {desc}: fluid {P.n}, wall {B.n}, DEM {D.n}, DEM wall {W.n}")
 
@@ -293,7 +338,8 @@ def gpu_arm(args, rank, world, local_rank):
         "data": "synthetic (seeded generator rules of the reference's input_gen)",
         "config": {"workload": desc, "fluid": P.n, "wall": B.n, "dem": D.n, "dem_wall": W.n,
                    "particles_counted": "fluid + moving DEM", "parallelism": f"replicas x{world}",
-                   "cell_factor": args.cell_factor,
+                   "cell_factor": args.cell_factor, "members": getattr(runner, "ninst", 1),
+                   "tuning": {k: v for k, v in tuning.items() if k != "ms_per_step"} or "defaults",
                    "l2": "state > 129 MB L2 (no flush)" if args.workload == "large800k"
                    else "state < L2 (resident between steps, as in a run)"},
         "e2e": {"value": job_throughput(n_units, e2e_steps, world, e2e_ms), "unit": "particle-steps/s",
@@ -308,7 +354,14 @@ def gpu_arm(args, rank, world, local_rank):
         "clocks": clocks.summary(),
     }
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        result["cpu_baseline"] = cpu_baseline(gen, solv, (P, B, D, W), scales, args.cpu_budget_s)
+        if args.workload == "batch64":
+            # members are independent: the oracle times member 0 (same particle-steps/s per core)
+            g0, s0, parts0, _ = make_case("batch64", "cpu")
+            result["cpu_baseline"] = cpu_baseline(g0, s0, parts0, dem_search_scales(parts0[2], parts0[3]),
+                                                  args.cpu_budget_s)
+            result["cpu_baseline"]["sample"] += " (ensemble member 0; members are independent)"
+        else:
+            result["cpu_baseline"] = cpu_baseline(gen, solv, (P, B, D, W), scales, args.cpu_budget_s)
     return result
 
 
@@ -403,7 +456,9 @@ def main():
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
-    ap.add_argument("--workload", default="large800k", choices=("large800k", "scaled"))
+    ap.add_argument("--workload", default="large800k", choices=WORKLOADS)
+    ap.add_argument("--autotune", action="store_true",
+                    help="time the launch candidates first (cached per case and GPU) and run the fastest")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPHDEM_ABI_VERSION 3
+#define SPHDEM_ABI_VERSION 4
 
 /* ---- return codes ---------------------------------------------------- */
 #define SPHDEM_OK                0
@@ -216,6 +216,12 @@ typedef struct sphdem_params {
     float boundary_radius_max;
     float h_max;             /* largest DEM coupling h                        */
     float h_uniform;         /* common DEM h, or 0 if heterogeneous           */
+    /* launch tuning (no effect on results): threads per block of the fluid and
+     * wall neighbour loops (64, 128 or 256; 0 = 128), and the porosity
+     * normaliser implementation (0 = direct loads, one warp per particle;
+     * 1 = shared-memory staged with TMA bulk copies, single-instance grids). */
+    int32_t block_sph;
+    int32_t porosity_variant;
 } sphdem_params_t;
 
 /* Everything one step touches. */

@@ -67,7 +67,8 @@ class WorkT(C.Structure):
 class ParamsT(C.Structure):
     _fields_ = [(n, C.c_float) for n in ("h", "support", "rho0", "c0", "gamma", "mu", "g", "dt")] + [
         ("shepard_step", C.c_int32)] + [(n, C.c_float) for n in (
-            "porosity_min", "porosity_max", "radius_max", "boundary_radius_max", "h_max", "h_uniform")]
+            "porosity_min", "porosity_max", "radius_max", "boundary_radius_max", "h_max", "h_uniform")] + [
+        ("block_sph", C.c_int32), ("porosity_variant", C.c_int32)]
 
 
 class CtxT(C.Structure):
@@ -83,7 +84,7 @@ FLAG_CSR_DEM_OVERFLOW = 0x1
 FLAG_CSR_BND_OVERFLOW = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_TIMEOUT = 0x10
-ABI_VERSION = 3
+ABI_VERSION = 4
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
 REL = dict(SPH_SPH_SUPPORT=0, SPH_BND_SUPPORT=1, BND_SPH_SUPPORT=2, BND_BND_SUPPORT=3, SPH_SPH_FORCE=4,

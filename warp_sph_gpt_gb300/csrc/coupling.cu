@@ -15,9 +15,6 @@
 //   k_react           Kernel_interaction_sph (:190-226) fused with
 //                     Kernel_step_sph (kernel/KERNEL_step.py:6-22).
 // Sums use fixed lane/warp orders, so every result is deterministic.
-#include <stdlib.h>
-#include <string.h>
-
 #include "common.cuh"
 #include "tma.cuh"
 
@@ -169,15 +166,18 @@ __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
 
 // ---------------------------------------------------------------------------
 // Porosity pass 2 for a uniform DEM h: shared-memory staged.  A CTA of 8 warps
-// takes 32 consecutive listed particles (4 per warp; neighbours in space),
-// trims the columns of their common query window to the ball around their
-// bounding box, and streams the candidate ranges through two shared buffers:
-// each buffer is packed with as many ranges (or range pieces) as fit, each
-// piece one 1D TMA bulk copy (cp.async.bulk), all completing on the buffer's
-// mbarrier; the next buffer fills while the current one is consumed.  Every
-// staged candidate is tested against the warp's 4 particles.  The candidate in
-// slot j is always handled by lane j % 32, in slot order, so each particle's
-// sum does not depend on how particles were grouped or buffers packed.
+// takes kGroup consecutive listed particles (kSubjPerWarp per warp; neighbours
+// in space), trims the columns of their common query window to the ball
+// around their bounding box, and streams the candidate ranges through two
+// shared buffers: each buffer is packed with as many ranges (or range pieces)
+// as fit, each piece one 1D TMA bulk copy (cp.async.bulk), all completing on
+// the buffer's mbarrier; the next buffer fills while the current one is
+// consumed.  Every staged candidate is tested against the warp's particles.
+// The candidate in slot j is always handled by lane j % 32, in slot order, so
+// each particle's sum does not depend on how particles were grouped or buffers
+// packed.  (Measured slower than k_porosity_near on GB300 for the dam-break
+// cases -- the sum is bound by FP32 issue, not by load latency -- so it is
+// the second choice of the launch tuning.)
 // ---------------------------------------------------------------------------
 constexpr int kTileWarps = 8;
 constexpr int kTileThreads = kTileWarps * 32;
@@ -512,7 +512,8 @@ CplArgs make_args(const sphdem_ctx_t* c, float support, float h) {
 
 }  // namespace
 
-int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st) {
+int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st,
+                 int variant) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     CplArgs a = make_args(c, support, h);
@@ -529,12 +530,9 @@ int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, f
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         // Two implementations of the uniform-h sum (same results, see the
-        // kernels); SPHDEM_POROSITY_KERNEL=staged selects the shared-memory
-        // staged one.  Grouped staging needs one instance per group.
-        static const bool staged = [] {
-            const char* v = getenv("SPHDEM_POROSITY_KERNEL");
-            return v && strcmp(v, "staged") == 0;
-        }();
+        // kernels); variant 1 selects the shared-memory staged one, which
+        // needs one instance per group of particles.
+        const bool staged = variant == 1;
         if (staged && h > 0.0f && c->grid_sph.ninst <= 1) {
             const int need = blocks_for(n, kGroup);
             int blocks = sms * 4;  // resident CTAs of k_porosity_tiles per SM

@@ -39,7 +39,7 @@ struct DensArgs {
 };
 
 template <bool FLT, bool RHO, bool PRES>
-__global__ void __launch_bounds__(128) k_density(DensArgs a) {
+__global__ void __launch_bounds__(256) k_density(DensArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n) return;
     const int o = a.gs.order[k];
@@ -100,7 +100,7 @@ struct WallArgs {
 };
 
 template <bool PRES>
-__global__ void __launch_bounds__(128) k_density_wall(WallArgs a) {
+__global__ void __launch_bounds__(256) k_density_wall(WallArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n) return;
     const int o = a.gb.order[k];
@@ -172,7 +172,7 @@ __device__ __forceinline__ void force_pair(const ForceArgs& a, const D2& r, cons
 }
 
 template <int MODE>
-__global__ void __launch_bounds__(128) k_force(ForceArgs a) {
+__global__ void __launch_bounds__(256) k_force(ForceArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.n) return;
     const int o = a.gs.order[k];
@@ -223,8 +223,11 @@ __global__ void k_step_sph(float* pos, float* vel, const float* __restrict__ acc
 
 static float tait_B(float rho0, float c0, float gamma) { return rho0 * c0 * c0 / gamma; }
 
+// Threads per block of the neighbour loops: 64, 128 or 256 (default 128).
+static int launch_block(int b) { return (b == 64 || b == 256) ? b : 128; }
+
 int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
-                float gamma, cudaStream_t st) {
+                float gamma, cudaStream_t st, int block) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     DensArgs a;
@@ -247,22 +250,22 @@ int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rh
     a.rho0 = rho0;
     a.B = tait_B(rho0, c0, gamma);
     a.gamma = gamma;
-    const int nb = blocks_for(n, 128);
+    const int bs = launch_block(block), nb = blocks_for(n, bs);
     if (flt && rho && pres)
-        k_density<true, true, true><<<nb, 128, 0, st>>>(a);
+        k_density<true, true, true><<<nb, bs, 0, st>>>(a);
     else if (!flt && rho && pres)
-        k_density<false, true, true><<<nb, 128, 0, st>>>(a);
+        k_density<false, true, true><<<nb, bs, 0, st>>>(a);
     else if (flt && !rho)
-        k_density<true, false, false><<<nb, 128, 0, st>>>(a);
+        k_density<true, false, false><<<nb, bs, 0, st>>>(a);
     else if (!flt && rho && !pres)
-        k_density<false, true, false><<<nb, 128, 0, st>>>(a);
+        k_density<false, true, false><<<nb, bs, 0, st>>>(a);
     else
-        k_density<true, true, false><<<nb, 128, 0, st>>>(a);
+        k_density<true, true, false><<<nb, bs, 0, st>>>(a);
     return launch_status("density");
 }
 
 int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, float rho0, float c0, float gamma,
-                     cudaStream_t st) {
+                     cudaStream_t st, int block) {
     const int n = c->bnd.n;
     if (n <= 0) return SPHDEM_OK;
     WallArgs a;
@@ -282,14 +285,15 @@ int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, f
     a.rho0 = rho0;
     a.B = tait_B(rho0, c0, gamma);
     a.gamma = gamma;
+    const int bs = launch_block(block);
     if (pres)
-        k_density_wall<true><<<blocks_for(n, 128), 128, 0, st>>>(a);
+        k_density_wall<true><<<blocks_for(n, bs), bs, 0, st>>>(a);
     else
-        k_density_wall<false><<<blocks_for(n, 128), 128, 0, st>>>(a);
+        k_density_wall<false><<<blocks_for(n, bs), bs, 0, st>>>(a);
     return launch_status("density_wall");
 }
 
-int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st) {
+int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st, int block) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     ForceArgs a;
@@ -312,13 +316,13 @@ int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, 
     a.two_mu = 2.0f * mu;
     a.eps_h2 = 0.01f * h * h;
     a.g = g;
-    const int nb = blocks_for(n, 128);
+    const int bs = launch_block(block), nb = blocks_for(n, bs);
     if (mode == 3)
-        k_force<3><<<nb, 128, 0, st>>>(a);
+        k_force<3><<<nb, bs, 0, st>>>(a);
     else if (mode == 2)
-        k_force<2><<<nb, 128, 0, st>>>(a);
+        k_force<2><<<nb, bs, 0, st>>>(a);
     else
-        k_force<1><<<nb, 128, 0, st>>>(a);
+        k_force<1><<<nb, bs, 0, st>>>(a);
     return launch_status("force");
 }
 

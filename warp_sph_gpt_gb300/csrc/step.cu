@@ -25,17 +25,19 @@ int gather_fluid(const sphdem_ctx_t* c, cudaStream_t st);
 int gather_wall(const sphdem_ctx_t* c, float support, float h, cudaStream_t st);
 int gather_wall_rho(const sphdem_ctx_t* c, cudaStream_t st);
 int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
-                float gamma, cudaStream_t st);
+                float gamma, cudaStream_t st, int block = 0);
 int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, float rho0, float c0, float gamma,
-                     cudaStream_t st);
-int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st);
+                     cudaStream_t st, int block = 0);
+int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st,
+              int block = 0);
 int run_pres(const float* rho, float* pres, int n, float rho0, float c0, float gamma, cudaStream_t st);
 int run_step_sph(const sphdem_ctx_t* c, float dt, cudaStream_t st);
 int run_contacts(const sphdem_ctx_t* c, float radius_max, float bnd_radius_max, float g, float dt, int which,
                  cudaStream_t st);
 int run_dem_aux(const sphdem_ctx_t* c, cudaStream_t st);
 int run_step_dem(const sphdem_ctx_t* c, float dt, cudaStream_t st);
-int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st);
+int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st,
+                 int variant = 0);
 int run_interaction_dem(const sphdem_ctx_t* c, float mu, float eps_min, float eps_max, float dt, cudaStream_t st);
 int run_react(const sphdem_ctx_t* c, float support, float dt, bool integrate, cudaStream_t st);
 int run_drag_beta(const float* eps, const float* rho, const float* mu, const float* d, const float* speed, int n,
@@ -76,11 +78,11 @@ bool shepard_due(const sphdem_params_t* p, int step) {
 // write_pgf; the acceleration arithmetic is the same either way.
 int sph_part(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool write_pgf, cudaStream_t st) {
     if (shep) TRY(gather_wall_rho(c, st));
-    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st));
-    TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st));
+    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph));
+    TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph));
     sphdem_ctx_t cc = *c;
     if (!write_pgf) cc.sph.pgf = nullptr;
-    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st);
+    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph);
 }
 
 int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integrate, cudaStream_t st) {
@@ -137,7 +139,7 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
     }
     TRY(sph_part(c, p, shep, true, st));
     const float support = 2.0f * p->h_max;  // source/Simulation.py:208
-    TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, st));
+    TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, st, p->porosity_variant));
     e = cudaStreamWaitEvent(st, f->join, 0);
     if (e != cudaSuccess) {
         set_error("join", e);
@@ -491,19 +493,20 @@ int sphdem_profile_step(sphdem_ctx_t* c, const sphdem_params_t* p, int step, int
         if (coupled && (rc = build_grid(&c->grid_dem, c->dem.pos, c->ctl, st))) break;
         mark();
         if (shep && (rc = gather_wall_rho(c, st))) break;
-        if ((rc = run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st))) break;
+        if ((rc = run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph))) break;
         mark();
-        if ((rc = run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st))) break;
+        if ((rc = run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph))) break;
         mark();
         sphdem_ctx_t cc = *c;
         if (!coupled) cc.sph.pgf = nullptr;
-        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st))) break;
+        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph))) break;
         mark();
         if (coupled && (rc = run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, st))) break;
         mark();
         const float support = 2.0f * p->h_max;
         if (coupled && ((rc = run_dem_aux(c, st)) ||
-                        (rc = run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, st))))
+                        (rc = run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, st,
+                                           p->porosity_variant))))
             break;
         mark();
         if (coupled && (rc = run_interaction_dem(c, p->mu, p->porosity_min, p->porosity_max, p->dt, st))) break;

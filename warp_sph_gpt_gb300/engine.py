@@ -47,6 +47,8 @@ class StepContext:
         self._sig = None
         self._status_host = torch.zeros(16, dtype=torch.int32, pin_memory=True)
         self._status_event = None
+        # launch tuning (results do not depend on it): see autotune.py
+        self.tuning = {"block_sph": 0, "porosity_variant": 0}
         self._alloc_work()
         addr = C.addressof(self.ctx)
         weakref.finalize(self, _release, self.lib, addr)
@@ -160,6 +162,8 @@ class StepContext:
         p.porosity_max = getattr(solv, "dem_porosity_max", 1.0)
         if scales is not None:
             p.radius_max, p.boundary_radius_max, p.h_max, p.h_uniform = (float(x) for x in scales)
+        p.block_sph = int(self.tuning.get("block_sph", 0))
+        p.porosity_variant = int(self.tuning.get("porosity_variant", 0))
 
     @property
     def stream(self):
