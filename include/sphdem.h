@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPHDEM_ABI_VERSION 4
+#define SPHDEM_ABI_VERSION 5
 
 /* ---- return codes ---------------------------------------------------- */
 #define SPHDEM_OK                0

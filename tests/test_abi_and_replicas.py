@@ -1,7 +1,7 @@
 """C ABI surface and the replica aggregation of bench.py (no GPU).
 
 * libsphdem.so loads without a GPU, reports its ABI version and exports every
-  function declared in include/sphdem.h; the ctypes mirrors of the ABI structs
+  function declared in include/*.h; the ctypes mirrors of the ABI structs
   have the library's own sizes.
 * bench.py --gpus N runs N independent replicas (the step does not shard);
   the job time is the max over ranks, checked here with two gloo ranks.
@@ -32,9 +32,11 @@ def lib():
 
 
 def declared_functions():
-    text = (ROOT / "include" / "sphdem.h").read_text()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(sphdem_\w+)\s*\(", text, flags=re.M))
+    names = set()
+    for header in sorted((ROOT / "include").glob("*.h")):
+        text = re.sub(r"/\*.*?\*/", "", header.read_text(), flags=re.S)
+        names |= set(re.findall(r"^\s*(?:int|int64_t|const char\*)\s+(sphdem_\w+)\s*\(", text, flags=re.M))
+    return names
 
 
 def test_library_loads_and_exports_every_declared_symbol(lib):
@@ -43,7 +45,7 @@ def test_library_loads_and_exports_every_declared_symbol(lib):
     names = declared_functions()
     assert len(names) >= 30
     for name in sorted(names):
-        assert hasattr(lib, name), f"{name} declared in include/sphdem.h but not exported"
+        assert hasattr(lib, name), f"{name} declared in include/*.h but not exported"
     assert set(_lib.EXPORTED) == names  # the binding covers exactly the declared surface
     assert lib.sphdem_abi_version() == _lib.ABI_VERSION
     _lib.check_layout(lib)  # raises on any size mismatch

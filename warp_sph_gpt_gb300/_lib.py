@@ -1,4 +1,4 @@
-"""ctypes binding of libsphdem.so (include/sphdem.h).
+"""ctypes binding of libsphdem.so (include/sphdem.h, include/sphdem_mpnn.h).
 
 The structures below mirror the C ABI field for field; ``check_layout`` compares
 their sizes with the library's own ``sizeof`` values at load time.  Loading
@@ -77,14 +77,41 @@ class CtxT(C.Structure):
                 ("ctl", C.c_void_p)]
 
 
-_MIRRORS = (SphT, BndT, CsrT, DemT, DemBndT, GridT, CtlT, WorkT, ParamsT, CtxT)
+c_u16_p = C.POINTER(C.c_uint16)
+
+
+class MpnnNodesT(C.Structure):
+    _fields_ = ([(n, c_float_p) for n in ("f_pos", "f_vel", "f_acc", "f_rho", "f_por")] + [("n_fluid", C.c_int32)]
+                + [(n, c_float_p) for n in ("d_pos", "d_vel", "d_acc", "d_rad")] + [("n_dem", C.c_int32)]
+                + [(n, c_float_p) for n in ("b_pos", "b_rho")] + [("n_wall", C.c_int32)]
+                + [(n, c_float_p) for n in ("w_pos", "w_rad")] + [("n_dem_wall", C.c_int32)]
+                + [(n, C.c_float) for n in ("rho0", "inv_vscale", "inv_ascale", "inv_radius")]
+                + [(n, c_float_p) for n in ("node_pos3", "node_pos4", "node_vel4")] + [("x", c_u16_p)])
+
+
+class MpnnNetT(C.Structure):
+    _fields_ = ([(n, C.c_int32) for n in ("n_nodes", "n_recv", "edge_capacity", "pad0")]
+                + [(n, C.c_float) for n in ("inv_radius", "inv_vscale", "inv_norm", "pad1")]
+                + [("node_pos4", c_float_p), ("node_vel4", c_float_p), ("x", c_u16_p), ("offset", c_int_p),
+                   ("sender", c_int_p), ("receiver", c_int_p), ("theta", c_float_p), ("packed", c_u16_p),
+                   ("z0", c_float_p), ("h0", c_u16_p), ("agg", c_float_p), ("h1", c_u16_p), ("z2", c_float_p),
+                   ("h2", c_u16_p), ("h3", c_u16_p), ("out", c_float_p), ("status", c_int_p)])
+
+
+class MpnnGradT(C.Structure):
+    _fields_ = [("d_out", c_float_p), ("g2", c_float_p), ("d_h2", c_float_p), ("d_h1", c_float_p),
+                ("d_h0", c_float_p), ("bf_a", c_u16_p), ("bf_b", c_u16_p), ("partial", c_float_p),
+                ("grad", c_float_p)]
+
+
+_MIRRORS = (SphT, BndT, CsrT, DemT, DemBndT, GridT, CtlT, WorkT, ParamsT, CtxT, MpnnNodesT, MpnnNetT, MpnnGradT)
 
 # Flags and codes of include/sphdem.h
 FLAG_CSR_DEM_OVERFLOW = 0x1
 FLAG_CSR_BND_OVERFLOW = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_TIMEOUT = 0x10
-ABI_VERSION = 4
+ABI_VERSION = 5
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
 REL = dict(SPH_SPH_SUPPORT=0, SPH_BND_SUPPORT=1, BND_SPH_SUPPORT=2, BND_BND_SUPPORT=3, SPH_SPH_FORCE=4,
@@ -124,9 +151,27 @@ _SIGNATURES = {
     "sphdem_neighbour_digest": ([C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p],
                                 C.c_int),
     "sphdem_diagnostics": ([C.c_void_p, C.c_float, C.c_void_p, C.c_void_p], C.c_int),
+    # include/sphdem_mpnn.h
+    "sphdem_mpnn_partial_floats": ([], C.c_int64),
+    "sphdem_mpnn_pack": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_mpnn_nodes": ([C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_mpnn_graph": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_float] + [C.c_void_p] * 3
+                          + [C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_mpnn_forward": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "sphdem_mpnn_backward": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_mpnn_loss": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_mpnn_adam": ([C.c_void_p] * 4 + [C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32,
+                                             C.c_void_p], C.c_int),
+    "sphdem_mpnn_apply": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
+                           C.c_int32, C.c_void_p, C.c_int32, C.c_float] + [C.c_void_p] * 5, C.c_int),
+    "sphdem_mpnn_maxdev": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_mpnn_gemm": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
+                          C.c_void_p], C.c_int),
+    "sphdem_mpnn_wgrad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
+                           C.c_void_p], C.c_int),
 }
 
-# Symbols declared in include/sphdem.h (checked by the CPU test suite).
+# Symbols declared in include/*.h (checked by the CPU test suite).
 EXPORTED = tuple(_SIGNATURES)
 
 
@@ -164,6 +209,8 @@ def load(path: Path | None = None):
 def check_layout(lib) -> None:
     sizes = (C.c_int64 * 16)()
     n = lib.sphdem_struct_sizes(sizes, 16)
+    if n != len(_MIRRORS):
+        raise RuntimeError(f"libsphdem reports {n} ABI structs, binding has {len(_MIRRORS)}")
     for k, mirror in enumerate(_MIRRORS[:n]):
         if C.sizeof(mirror) != sizes[k]:
             raise RuntimeError(f"ctypes mirror {mirror.__name__} has size {C.sizeof(mirror)}, "

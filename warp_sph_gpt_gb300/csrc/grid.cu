@@ -77,6 +77,13 @@ __global__ void k_scan_add(int* __restrict__ data, int n, const int* __restrict_
     if (i == 0) data[n] = total_points;
 }
 
+// As k_scan_add, with data[n] = the grand total left by k_scan_sums.
+__global__ void k_scan_add_total(int* __restrict__ data, int n, const int* __restrict__ sums, int nb) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) data[i] += sums[i / kScanTile];
+    if (i == 0) data[n] = sums[nb];
+}
+
 __global__ void k_scatter(const int* __restrict__ key, int n, const int* __restrict__ start, int* __restrict__ cursor,
                           int* __restrict__ order) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -152,6 +159,16 @@ int scan_cells(int* data, int ncell, int total_points, int* sums, cudaStream_t s
 }
 
 }  // namespace
+
+// Exclusive scan of n counts in place, data[n] = their total (device side).
+int scan_counts(int* data, int n, int* sums, cudaStream_t st) {
+    int nb = (n + kScanTile - 1) / kScanTile;
+    if (nb < 1) nb = 1;
+    k_scan_tiles<<<nb, kScanThreads, 0, st>>>(data, n, sums);
+    k_scan_sums<<<1, 1024, 0, st>>>(sums, nb);
+    k_scan_add_total<<<blocks_for(n > 0 ? n : 1, 256), 256, 0, st>>>(data, n, sums, nb);
+    return launch_status("scan_counts");
+}
 
 // Bin + scan + scatter + stable per-cell sort of the points of one grid.
 int build_grid(sphdem_grid_t* g, const float* pos, sphdem_ctl_t* ctl, cudaStream_t st) {

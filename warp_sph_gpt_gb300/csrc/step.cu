@@ -17,6 +17,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "sphdem_mpnn.h"
 
 namespace sd {
 
@@ -389,7 +390,9 @@ int sphdem_struct_sizes(int64_t* out, int n) {
                          (int64_t)sizeof(sphdem_csr_t),   (int64_t)sizeof(sphdem_dem_t),
                          (int64_t)sizeof(sphdem_dembnd_t), (int64_t)sizeof(sphdem_grid_t),
                          (int64_t)sizeof(sphdem_ctl_t),   (int64_t)sizeof(sphdem_work_t),
-                         (int64_t)sizeof(sphdem_params_t), (int64_t)sizeof(sphdem_ctx_t)};
+                         (int64_t)sizeof(sphdem_params_t), (int64_t)sizeof(sphdem_ctx_t),
+                         (int64_t)sizeof(sphdem_mpnn_nodes_t), (int64_t)sizeof(sphdem_mpnn_net_t),
+                         (int64_t)sizeof(sphdem_mpnn_grad_t)};
     const int m = (int)(sizeof(s) / sizeof(s[0]));
     for (int i = 0; i < n && i < m; ++i) out[i] = s[i];
     return m;
