@@ -67,7 +67,7 @@ def log(*a):
 # ---------------------------------------------------------------------------
 # workloads
 # ---------------------------------------------------------------------------
-WORKLOADS = ("large800k", "scaled", "batch64")
+WORKLOADS = ("large800k", "scaled", "small", "batch64", "learned")
 BATCH_MEMBERS = 64
 
 
@@ -81,6 +81,11 @@ def _case_spec(workload: str):
     elif workload == "scaled":
         gen, pos, rad = config_scaled(seed=0)
         desc = "scaled dam break: tank 2x0.4x1 m, fluid 0.5x0.4x0.5 m at dx=0.01, 160 DEM R=0.025, dt=5e-5"
+    elif workload == "small":
+        from warp_sph_gpt_gb300.generate import config_small
+
+        gen, pos, rad = config_small(), None, None
+        desc = "config-1 dam break: the reference's input files (12,500 fluid, 48,336 wall, 20 DEM), dt=1e-4"
     else:
         raise SystemExit(f"unknown workload {workload}")
     return gen, pos, rad, desc
@@ -93,11 +98,22 @@ def make_case(workload: str, device):
     if workload == "batch64":
         gen, pos, rad = config_batch_member(0)
         desc = f"batch member 0 of {BATCH_MEMBERS}"
+    elif workload == "learned":
+        from warp_sph_gpt_gb300.generate import config_small
+
+        gen, pos, rad = config_small(), None, None
+        desc = "config-1 dam break (12,500 fluid, 20 DEM), plain method"
     else:
         gen, pos, rad, desc = _case_spec(workload)
     P, B, D, W = build_case(gen, pos, rad, device=device)
     solv = solver_config(gen)
     return gen, solv, (P, B, D, W), desc
+
+
+def default_lanes(n_fluid: int) -> int:
+    """One warp per particle for small systems (one thread each leaves most
+    SMs idle), one thread per particle otherwise."""
+    return 32 if n_fluid <= 50_000 else 1
 
 
 def make_runner(workload: str, device, cell_factor: float = 1.0):
@@ -229,15 +245,17 @@ def gpu_arm(args, rank, world, local_rank):
 
         probe = make_runner(args.workload, device)
         key = case_key(probe.P, probe.B, probe.D, probe.W, probe.ninst)
+        n_fluid = probe.P.n
         del probe
         tuning = autotune(lambda cf: make_runner(args.workload, device, cf), key,
-                          ninst=BATCH_MEMBERS if args.workload == "batch64" else 1, log=log)
+                          ninst=BATCH_MEMBERS if args.workload == "batch64" else 1, log=log, n_fluid=n_fluid)
         args.cell_factor = tuning["cell_factor"]
         log(f"[rank {rank}] autotuned: {tuning}")
         torch.cuda.empty_cache()
     runner = make_runner(args.workload, device, args.cell_factor)
-    if tuning:
-        runner.tune(tuning)
+    if not tuning:
+        tuning = {"lanes_sph": default_lanes(runner.P.n)}
+    runner.tune(tuning)
     gen, solv, desc = runner.gen, runner.solv, runner.desc
     P, B, D, W = runner.P, runner.B, runner.D, runner.W
     scales, grids = runner.scales, runner.grids
@@ -339,7 +357,7 @@ def gpu_arm(args, rank, world, local_rank):
         "config": {"workload": desc, "fluid": P.n, "wall": B.n, "dem": D.n, "dem_wall": W.n,
                    "particles_counted": "fluid + moving DEM", "parallelism": f"replicas x{world}",
                    "cell_factor": args.cell_factor, "members": getattr(runner, "ninst", 1),
-                   "tuning": {k: v for k, v in tuning.items() if k != "ms_per_step"} or "defaults",
+                   "tuning": {k: v for k, v in tuning.items() if k != "ms_per_step"},
                    "l2": "state > 129 MB L2 (no flush)" if args.workload == "large800k"
                    else "state < L2 (resident between steps, as in a run)"},
         "e2e": {"value": job_throughput(n_units, e2e_steps, world, e2e_ms), "unit": "particle-steps/s",
@@ -363,6 +381,182 @@ def gpu_arm(args, rank, world, local_rank):
         else:
             result["cpu_baseline"] = cpu_baseline(gen, solv, (P, B, D, W), scales, args.cpu_budget_s)
     return result
+
+
+# ---------------------------------------------------------------------------
+# learned surrogate vs plain on the config-1 dam break
+# ---------------------------------------------------------------------------
+def _fluid_density(case):
+    from warp_sph_gpt_gb300.kernels import Kernel_density_sph
+
+    Kernel_density_sph(case.P, case.B, case.grids[0], case.grids[1], case.solv.support, case.solv.h)
+    return case.P.rho.clone()
+
+
+def _edge_flops(E, nn, nr):
+    """Tensor-core FLOPs of one forward pass: two edge passes (16->128->128 per
+    edge) and the node layers (16->128, 128->128 on all nodes, 128->16 on
+    receivers)."""
+    return 2 * E * 2 * (16 * 128 + 128 * 128) + nn * 2 * (16 * 128 + 128 * 128) + nr * 2 * 128 * 16
+
+
+def learned_arm(args, rank, world, local_rank):
+    import torch
+
+    from warp_sph_gpt_gb300 import surrogate as S
+    from warp_sph_gpt_gb300.batch import Case, Ensemble
+    from warp_sph_gpt_gb300.generate import config_batch_member, config_small
+
+    torch.cuda.set_device(local_rank)
+    device = torch.device("cuda", local_rank)
+    t_start = time.perf_counter()
+    # training data: trajectories of the batched plain solver (seeded dx = 0.02 dam breaks)
+    members = [config_batch_member(1000 + i) for i in range(args.train_members)]
+    ens = Ensemble(members, device=device)
+    s = ens.solv
+    cfg = S.SurrogateConfig(radius=float(args.graph_radius or s.support), dt=float(s.dt), rho0=float(s.rho0),
+                            tol=args.judge_tol, judge=args.judge)
+    t0 = time.perf_counter()
+    ts = S.generate(ens, args.train_steps, cfg, log=log)
+    t_gen = time.perf_counter() - t0
+    n_val = max(1, len(members) // 8)
+    train_ids = list(range(len(members) - n_val))
+    val_ids = list(range(len(members) - n_val, len(members)))
+    S.fit_scales(ts, cfg, train_ids[:16], device)
+    net = S.Network(cfg, device, seed=0)
+    prior = S.evaluate(net, ts, val_ids, zero=True)
+    t0 = time.perf_counter()
+    hist = S.train(net, ts, train_ids, iters=args.train_iters, lr=2e-3, log=log, log_every=500)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t0
+    val = S.evaluate(net, ts, val_ids)
+    log(f"held-out one-jump loss: prior {prior:.4f} -> trained {val:.4f}")
+    del ts, ens
+    torch.cuda.empty_cache()
+
+    n = args.rollout_steps
+    K = cfg.substeps + 1
+    dx = 0.02
+    # plain: graph replay of the coupled step
+    plain = Case(config_small(), device=device)
+    plain.tune({"lanes_sph": default_lanes(plain.P.n)})
+    snap0 = plain.snapshot()
+    plain.run(0, 3 * K)
+    torch.cuda.synchronize()
+    plain.restore(snap0)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks_plain:
+        e0.record()
+        plain.run(0, n)
+        e1.record()
+        torch.cuda.synchronize()
+    t_plain = e0.elapsed_time(e1) * 1e-3
+    pos_p, vel_p = plain.P.pos.clone(), plain.P.vel.clone()
+    dpos_p = plain.D.pos.clone()
+    rho_p = _fluid_density(plain)
+    # the plain method's own density deviation at every jump boundary (untimed re-run)
+    plain_final = plain.snapshot()
+    plain.restore(snap0)
+    plain_dev = []
+    for s0 in range(0, n, K):
+        plain.run(s0, min(K, n - s0))
+        plain_dev.append((plain.P.rho - cfg.rho0).abs().max().item() / cfg.rho0)
+    plain.restore(plain_final)
+    # learned: one plain step + m learned substeps per jump, density judge, plain fallback
+    learned = Case(config_small(), device=device)
+    learned.tune({"lanes_sph": default_lanes(learned.P.n)})
+    snapL = learned.snapshot()
+    ro = S.LearnedRollout(learned, net)
+    ro.run(0, 6 * K)  # both Shepard variants run eagerly once, then are captured
+    torch.cuda.synchronize()
+    learned.restore(snapL)
+    ro.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0)
+    # e2e: initial state from pinned host memory, final state back to the host
+    host_in = {k: t.detach().cpu().pin_memory() for k, t in (("pos", learned.P.pos), ("vel", learned.P.vel),
+                                                              ("dpos", learned.D.pos), ("dvel", learned.D.vel))}
+    host_out = {k: torch.empty_like(v).pin_memory() for k, v in host_in.items()}
+    h2d = sum(v.numel() * v.element_size() for v in host_in.values())
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks_learned:
+        torch.cuda.nvtx.range_push("learned_rollout")
+        t0 = time.perf_counter()
+        learned.P.pos.copy_(host_in["pos"], non_blocking=True)
+        learned.P.vel.copy_(host_in["vel"], non_blocking=True)
+        learned.D.pos.copy_(host_in["dpos"], non_blocking=True)
+        learned.D.vel.copy_(host_in["dvel"], non_blocking=True)
+        stats = ro.run(0, n)
+        host_out["pos"].copy_(learned.P.pos, non_blocking=True)
+        host_out["vel"].copy_(learned.P.vel, non_blocking=True)
+        host_out["dpos"].copy_(learned.D.pos, non_blocking=True)
+        host_out["dvel"].copy_(learned.D.vel, non_blocking=True)
+        torch.cuda.synchronize()
+        t_learned = time.perf_counter() - t0
+        torch.cuda.nvtx.range_pop()
+    err = (learned.P.pos - pos_p).norm(dim=1) / dx
+    derr = (learned.D.pos - dpos_p).norm(dim=1) / dx if learned.D.n else torch.zeros(1, device=device)
+    rho_l = _fluid_density(learned)
+    rho_dev = ((rho_l - rho_p).abs().max() / cfg.rho0).item()
+    rho_rms = ((rho_l - rho_p).pow(2).mean().sqrt() / cfg.rho0).item()
+    # tensor-core roofline of the network's forward pass on the final state
+    g = ro.g
+    g.set_nodes(S.Sets(learned.P, learned.B, learned.D, learned.W))
+    g.build()
+    E = g.n_edges()
+    g.forward(net)
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_push("mpnn_forward")
+    f0.record()
+    for _ in range(reps):
+        g.forward(net)
+    f1.record()
+    torch.cuda.synchronize()
+    torch.cuda.nvtx.range_pop()
+    fwd_ms = f0.elapsed_time(f1) / reps
+    flops = _edge_flops(E, g.n_nodes, g.n_recv)
+    peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
+    peak_tf = float(peaks.get("bf16_tflops", 1900.0))
+    achieved_tf = flops / (fwd_ms * 1e-3) / 1e12
+    units = learned.P.n + learned.D.n
+    value = units * n / t_learned
+    return {
+        "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": n, "warmup": 6 * K, "ms_per_step": t_learned * 1e3 / n, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "bf16 network (fp32 accumulate) + f32 plain steps",
+        "data": "synthetic (seeded generator rules; training trajectories from the batched plain solver)",
+        "config": {"workload": "learned K-step surrogate vs plain on the config-1 dam break "
+                               "(12,500 fluid, 20 DEM, dt=1e-4)", "K": K, "judge_tol": cfg.tol, "judge": cfg.judge,
+                   "graph_radius": cfg.radius,
+                   "rollout_steps": n, "fluid": learned.P.n, "dem": learned.D.n,
+                   "l2": "state < L2 (resident between steps, as in a run)"},
+        "plain": {"value": units * n / t_plain, "ms_per_step": t_plain * 1e3 / n, "clocks": clocks_plain.summary()},
+        "speedup_vs_plain": t_plain / t_learned,
+        "error_vs_plain": {"pos_max_dx": err.max().item(), "pos_rms_dx": err.pow(2).mean().sqrt().item(),
+                           "dem_pos_max_dx": derr.max().item(), "rho_max_diff": rho_dev, "rho_rms_diff": rho_rms,
+                           "learned_final_density_deviation": ((rho_l - cfg.rho0).abs().max() / cfg.rho0).item(),
+                           "plain_final_density_deviation": ((rho_p - cfg.rho0).abs().max() / cfg.rho0).item(),
+                           "judge_max_dev_accepted": stats["max_dev_accepted"]},
+        "plain_density_deviation": {"max": max(plain_dev), "mean": sum(plain_dev) / len(plain_dev),
+                                    "fraction_above_tol": sum(d > cfg.tol for d in plain_dev) / len(plain_dev)},
+        "rollout": stats,
+        "training": {"members": len(members), "train_members": len(train_ids), "val_members": len(val_ids),
+                     "trajectory_steps": args.train_steps, "iterations": args.train_iters,
+                     "generate_s": round(t_gen, 2), "train_s": round(t_train, 2),
+                     "val_loss_prior": prior, "val_loss_trained": val, "loss_history": hist[-3:]},
+        "roofline": {"bound": "tensor", "kernel_phase": "mpnn forward (k_rows, k_edges)", "achieved": achieved_tf,
+                     "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
+                     "peak_source": "measured" if peaks else "fallback", "flops_per_launch": flops,
+                     "edges": E, "forward_ms": fwd_ms, "traffic": None},
+        "e2e": {"value": units * n / t_learned, "unit": "particle-steps/s", "h2d_bytes_per_step": h2d / n,
+                "d2h_bytes_per_step": h2d / n,
+                "api": "LearnedRollout.run over the whole rollout; initial state from pinned host memory, final "
+                       "state back"},
+        "gpu_launches": None,
+        "clocks": clocks_learned.summary(),
+        "wall_s": round(time.perf_counter() - t_start, 1),
+    }
 
 
 # ---------------------------------------------------------------------------
@@ -457,6 +651,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=("gb300", "reference"))
     ap.add_argument("--workload", default="large800k", choices=WORKLOADS)
+    ap.add_argument("--train-members", type=int, default=64, help="learned: ensemble members of training data")
+    ap.add_argument("--train-steps", type=int, default=1000, help="learned: plain steps per training trajectory")
+    ap.add_argument("--train-iters", type=int, default=3000, help="learned: Adam iterations")
+    ap.add_argument("--rollout-steps", type=int, default=1000, help="learned: steps of the compared rollouts")
+    ap.add_argument("--judge-tol", type=float, default=0.01, help="learned: density judge tolerance / rho0")
+    ap.add_argument("--judge", type=int, default=1, choices=(0, 1),
+                    help="learned: 1 = density deviation |rho - rho0| / rho0, 0 = change over the jump")
+    ap.add_argument("--graph-radius", type=float, default=0.0, help="learned: edge radius (0 = SPH support)")
     ap.add_argument("--autotune", action="store_true",
                     help="time the launch candidates first (cached per case and GPU) and run the fastest")
     ap.add_argument("--e2e-steps", type=int, default=20)
@@ -481,7 +683,7 @@ def main():
         import torch.distributed as dist
 
         dist.init_process_group("nccl", init_method="env://")
-    result = gpu_arm(args, rank, world, local_rank)
+    result = (learned_arm if args.workload == "learned" else gpu_arm)(args, rank, world, local_rank)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if world > 1:

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPHDEM_ABI_VERSION 5
+#define SPHDEM_ABI_VERSION 6
 
 /* ---- return codes ---------------------------------------------------- */
 #define SPHDEM_OK                0
@@ -216,12 +216,17 @@ typedef struct sphdem_params {
     float boundary_radius_max;
     float h_max;             /* largest DEM coupling h                        */
     float h_uniform;         /* common DEM h, or 0 if heterogeneous           */
-    /* launch tuning (no effect on results): threads per block of the fluid and
-     * wall neighbour loops (64, 128 or 256; 0 = 128), and the porosity
-     * normaliser implementation (0 = direct loads, one warp per particle;
-     * 1 = shared-memory staged with TMA bulk copies, single-instance grids). */
+    /* launch tuning (neighbour sets unchanged; sums may change only by FP32
+     * summation order): threads per block of the fluid and wall neighbour
+     * loops (64, 128 or 256; 0 = 128), the porosity normaliser implementation
+     * (0 = direct loads, one warp per particle; 1 = shared-memory staged with
+     * TMA bulk copies, single-instance grids), and the lanes per subject of
+     * the density, wall-density and force loops (0/1 = one thread per
+     * particle; 32 = one warp per particle, for small systems). */
     int32_t block_sph;
     int32_t porosity_variant;
+    int32_t lanes_sph;
+    int32_t pad_params;
 } sphdem_params_t;
 
 /* Everything one step touches. */

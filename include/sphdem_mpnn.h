@@ -153,9 +153,45 @@ int sphdem_mpnn_apply(float* f_pos, float* f_vel, const float* f_acc, int32_t n_
                       const float* scale4, const float* x_t, const float* v_t, float* target,
                       sphdem_stream_t stream);
 
-/* max_i |a_i - b_i| * inv over n floats into *out (device, FP32, >= 0; must
- * start at 0). */
-int sphdem_mpnn_maxdev(const float* a, const float* b, int32_t n, float inv, float* out, sphdem_stream_t stream);
+/* max_i |a_i - b_i| * inv over n floats (b == NULL: b_i = ref) into *out
+ * (device, FP32, >= 0; must start at 0). */
+int sphdem_mpnn_maxdev(const float* a, const float* b, float ref, int32_t n, float inv, float* out,
+                       sphdem_stream_t stream);
+
+/* One learned jump, replayed from a CUDA graph per Shepard variant:
+ *   1. the loop body of sphdem_run for `step` (moving grids + coupled step);
+ *   2. backup of fluid/DEM positions and velocities and the fluid density
+ *      into `keep`;
+ *   3. node inputs, radius graph, forward pass, prior + correction of
+ *      `substeps` steps applied in place (sphdem_mpnn_apply);
+ *   4. the judge: fluid grid rebuilt and the filtered fluid density
+ *      evaluated at the new positions (the density pass of the plain step),
+ *      *dev = max_i |rho_new - rho_old| / rho0 (judge 0) or
+ *      max_i |rho_new - rho0| / rho0 (judge 1).
+ * The caller reads *dev (and net.status) and, above its tolerance, calls
+ * sphdem_jump_undo and runs the substeps with sphdem_run.  The plain step of
+ * 1. flips the DEM contact CSR parity once. */
+typedef struct sphdem_jump {
+    sphdem_mpnn_nodes_t nodes;  /* node inputs; the fluid/DEM/wall pointers are the context's */
+    sphdem_mpnn_net_t net;      /* network state; net.status points into graph_ctl */
+    sphdem_grid_t node_grid;    /* grid over nodes.node_pos3, cell >= radius */
+    int32_t* scan_scratch;      /* sphdem_scan_scratch(n_recv) words */
+    sphdem_ctl_t* graph_ctl;    /* device control block of the node grid and kernels */
+    float radius;
+    int32_t substeps;
+    float scale[4];             /* output scales, as sphdem_mpnn_apply's scale4 */
+    float* keep;                /* [6 n_fluid + 6 n_dem + n_fluid] backup */
+    float* dev;                 /* [1] judge result (device) */
+    int32_t judge;              /* 0: max |rho_new - rho_old| / rho0 (change over the jump);
+                                   1: max |rho_new - rho0| / rho0 (density deviation) */
+    int32_t pad_jump;
+} sphdem_jump_t;
+
+int sphdem_jump(sphdem_ctx_t* ctx, const sphdem_params_t* p, const sphdem_jump_t* j, int step,
+                sphdem_stream_t stream);
+
+/* Restore positions, velocities and fluid density saved by the last jump. */
+int sphdem_jump_undo(sphdem_ctx_t* ctx, const sphdem_jump_t* j, sphdem_stream_t stream);
 
 /* Tensor-core GEMM check: C[M,N] (FP32) = A[M,K] B[N,K]^T for BF16 row-major
  * A, B; K, N in {16, 128}. */

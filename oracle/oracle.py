@@ -54,7 +54,8 @@ class _Params(C.Structure):
     _fields_ = [(n, C.c_float) for n in ("h", "support", "rho0", "c0", "gamma", "mu", "g", "dt")] + [
         ("shepard_step", C.c_int32)] + [(n, C.c_float) for n in (
             "porosity_min", "porosity_max", "radius_max", "boundary_radius_max", "h_max", "h_uniform")] + [
-        ("block_sph", C.c_int32), ("porosity_variant", C.c_int32)]
+        ("block_sph", C.c_int32), ("porosity_variant", C.c_int32), ("lanes_sph", C.c_int32),
+        ("pad_params", C.c_int32)]
 
 
 SPH_FIELDS = (("pos", 3), ("vel", 3), ("rho_raw", 1), ("rho", 1), ("pres", 1), ("acc", 3), ("m", 1), ("flt", 1),

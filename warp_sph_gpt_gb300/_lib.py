@@ -68,7 +68,8 @@ class ParamsT(C.Structure):
     _fields_ = [(n, C.c_float) for n in ("h", "support", "rho0", "c0", "gamma", "mu", "g", "dt")] + [
         ("shepard_step", C.c_int32)] + [(n, C.c_float) for n in (
             "porosity_min", "porosity_max", "radius_max", "boundary_radius_max", "h_max", "h_uniform")] + [
-        ("block_sph", C.c_int32), ("porosity_variant", C.c_int32)]
+        ("block_sph", C.c_int32), ("porosity_variant", C.c_int32), ("lanes_sph", C.c_int32),
+        ("pad_params", C.c_int32)]
 
 
 class CtxT(C.Structure):
@@ -104,14 +105,21 @@ class MpnnGradT(C.Structure):
                 ("grad", c_float_p)]
 
 
-_MIRRORS = (SphT, BndT, CsrT, DemT, DemBndT, GridT, CtlT, WorkT, ParamsT, CtxT, MpnnNodesT, MpnnNetT, MpnnGradT)
+class JumpT(C.Structure):
+    _fields_ = [("nodes", MpnnNodesT), ("net", MpnnNetT), ("node_grid", GridT), ("scan_scratch", c_int_p),
+                ("graph_ctl", C.c_void_p), ("radius", C.c_float), ("substeps", C.c_int32), ("scale", C.c_float * 4),
+                ("keep", c_float_p), ("dev", c_float_p), ("judge", C.c_int32), ("pad_jump", C.c_int32)]
+
+
+_MIRRORS = (SphT, BndT, CsrT, DemT, DemBndT, GridT, CtlT, WorkT, ParamsT, CtxT, MpnnNodesT, MpnnNetT, MpnnGradT,
+            JumpT)
 
 # Flags and codes of include/sphdem.h
 FLAG_CSR_DEM_OVERFLOW = 0x1
 FLAG_CSR_BND_OVERFLOW = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_TIMEOUT = 0x10
-ABI_VERSION = 5
+ABI_VERSION = 6
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
 REL = dict(SPH_SPH_SUPPORT=0, SPH_BND_SUPPORT=1, BND_SPH_SUPPORT=2, BND_BND_SUPPORT=3, SPH_SPH_FORCE=4,
@@ -164,9 +172,12 @@ _SIGNATURES = {
                                              C.c_void_p], C.c_int),
     "sphdem_mpnn_apply": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,
                            C.c_int32, C.c_void_p, C.c_int32, C.c_float] + [C.c_void_p] * 5, C.c_int),
-    "sphdem_mpnn_maxdev": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_float, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_mpnn_maxdev": ([C.c_void_p, C.c_void_p, C.c_float, C.c_int32, C.c_float, C.c_void_p, C.c_void_p],
+                           C.c_int),
     "sphdem_mpnn_gemm": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                           C.c_void_p], C.c_int),
+    "sphdem_jump": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "sphdem_jump_undo": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_mpnn_wgrad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                            C.c_void_p], C.c_int),
 }

@@ -21,6 +21,7 @@ from .input_reader import dem_search_scales
 from .simulation import SPHDEM_OneStep, run_steps
 from .struct import BNDptl, DEMBNDptl, DEMptl, SPHptl
 
+TUNING_KEYS = ("block_sph", "porosity_variant", "lanes_sph")
 _SOLVER_FIELDS = ("h", "support", "rho0", "c0", "gamma", "mu", "g", "dt", "shepard_step", "dem_porosity_min",
                   "dem_porosity_max")
 
@@ -39,7 +40,7 @@ class _Runner:
         from .engine import context_for
 
         ctx = context_for(self.P, self.B, self.D, self.W, tuple(self.grids))
-        ctx.tuning.update({k: int(v) for k, v in tuning.items() if k in ("block_sph", "porosity_variant")})
+        ctx.tuning.update({k: int(v) for k, v in tuning.items() if k in TUNING_KEYS})
 
     @property
     def n_units(self) -> int:
@@ -54,6 +55,34 @@ class _Runner:
     def step(self, step: int) -> None:
         """One coupled step through the step API."""
         SPHDEM_OneStep(self.solv, self.P, self.B, self.D, self.W, *self.grids, step, self.scales)
+
+    def snapshot(self) -> dict:
+        """Device copy of the whole dynamic state (every particle field, both
+        contact CSR sides, the control block and the host parity mirror)."""
+        snap = {}
+        for key, part in (("P", self.P), ("B", self.B), ("D", self.D), ("W", self.W)):
+            for name, _ in part._fields:
+                snap[(key, name)] = getattr(part, name).clone()
+        for kind, ck in self.D._kinds.items():
+            for si, side in enumerate(ck.sides):
+                for a in type(side).__slots__:
+                    snap[("csr", kind, si, a)] = getattr(side, a).clone()
+        snap["ctl"] = self.D._ctl.clone()
+        snap["old"] = dict(self.D._old)
+        return snap
+
+    def restore(self, snap: dict) -> None:
+        """Copy a snapshot back in place (buffers keep their addresses, so
+        contexts and captured graphs stay valid)."""
+        for key, part in (("P", self.P), ("B", self.B), ("D", self.D), ("W", self.W)):
+            for name, _ in part._fields:
+                getattr(part, name).copy_(snap[(key, name)])
+        for kind, ck in self.D._kinds.items():
+            for si, side in enumerate(ck.sides):
+                for a in type(side).__slots__:
+                    getattr(side, a).copy_(snap[("csr", kind, si, a)])
+        self.D._ctl.copy_(snap["ctl"])
+        self.D._old.update(snap["old"])
 
     def _make_grids(self, inst=None, cell_factor: float = 1.0) -> None:
         s, sc = self.solv, self.scales

@@ -9,6 +9,7 @@
 //   5. gather   sorted copies of the fields that neighbour loops read
 // Memory: cell_start [ncell+1], order/key [n], cursor [ncell] and scan scratch
 // are caller-owned tensors; nothing is allocated here.
+#include <limits.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -92,19 +93,51 @@ __global__ void k_scatter(const int* __restrict__ key, int n, const int* __restr
     order[start[k] + atomicAdd(cursor + k, 1)] = i;
 }
 
-// Stable order inside each cell: insertion sort of the (short) slot range.
-__global__ void k_sort_cells(const int* __restrict__ start, int ncell, int* __restrict__ order) {
-    int c = blockIdx.x * blockDim.x + threadIdx.x;
-    if (c >= ncell) return;
-    int s = start[c], e = start[c + 1];
-    for (int a = s + 1; a < e; ++a) {
-        int v = order[a];
-        int b = a - 1;
-        while (b >= s && order[b] > v) {
-            order[b + 1] = order[b];
-            --b;
+// Stable order inside each cell: the slots of a cell sorted by point index.
+// One thread checks each cell; the warp then sorts its lanes' cells that hold
+// 2..32 points one after another, each in registers by a bitonic network of
+// shuffles.  Longer cells (rare) fall back to an insertion sort by their lane.
+__device__ __forceinline__ int warp_bitonic_sort(int v, int lane) {
+#pragma unroll
+    for (int k = 2; k <= 32; k <<= 1) {
+#pragma unroll
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int o = __shfl_xor_sync(0xffffffffu, v, j);
+            const bool up = (lane & k) == 0;
+            const bool lower = (lane & j) == 0;
+            v = (lower == up) ? min(v, o) : max(v, o);
         }
-        order[b + 1] = v;
+    }
+    return v;
+}
+
+__global__ void k_sort_cells(const int* __restrict__ start, int ncell, int* __restrict__ order) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    int s = 0, n = 0;
+    if (c < ncell) {
+        s = start[c];
+        n = start[c + 1] - s;
+    }
+    unsigned todo = __ballot_sync(0xffffffffu, n >= 2 && n <= 32);
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const int cs = __shfl_sync(0xffffffffu, s, src), cn = __shfl_sync(0xffffffffu, n, src);
+        int v = lane < cn ? order[cs + lane] : INT_MAX;
+        v = warp_bitonic_sort(v, lane);
+        if (lane < cn) order[cs + lane] = v;
+    }
+    if (n > 32) {
+        for (int a = s + 1; a < s + n; ++a) {
+            int v = order[a];
+            int b = a - 1;
+            while (b >= s && order[b] > v) {
+                order[b + 1] = order[b];
+                --b;
+            }
+            order[b + 1] = v;
+        }
     }
 }
 

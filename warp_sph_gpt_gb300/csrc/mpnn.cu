@@ -53,9 +53,12 @@ static_assert(P_N3T + 2048 == SPHDEM_MPNN_PACKED, "packed layout");
 enum { EPI_F32 = 0, EPI_SILU = 1 };
 enum { MODE_AGG = 0, MODE_SCATTER = 1 };
 
-__device__ __forceinline__ float silu(float z) { return z / (1.0f + __expf(-z)); }
+// SiLU z * sigmoid(z) with the fast exponential and reciprocal (relative
+// error far below the BF16 rounding of the activations it feeds).
+__device__ __forceinline__ float sigmoid(float z) { return __frcp_rn(1.0f + __expf(-z)); }
+__device__ __forceinline__ float silu(float z) { return z * sigmoid(z); }
 __device__ __forceinline__ float silu_grad(float z) {
-    const float s = 1.0f / (1.0f + __expf(-z));
+    const float s = sigmoid(z);
     return s * (1.0f + z * (1.0f - s));
 }
 __device__ __forceinline__ uint32_t pack2(float a, float b) {
@@ -292,65 +295,154 @@ __device__ __forceinline__ void edge_features(const EdgeArgs& a, int e, int E, i
 
 constexpr uint32_t kImg16 = 128 * 16 * 2;   // 4 KB
 constexpr uint32_t kImg128 = 128 * 128 * 2;  // 32 KB
-// k_edges shared memory
-constexpr uint32_t EF_IMG1 = 0, EF_IMG2 = EF_IMG1 + kImg16, EF_XS = EF_IMG2 + kImg128, EF_ZR = EF_XS + kImg16,
-                   EF_B1 = EF_ZR + kImg128, EF_B2 = EF_B1 + 512, EF_SR = EF_B2 + 512, EF_SJ = EF_SR + 512,
-                   EF_BARS = EF_SJ + 512, EF_SLOT = EF_BARS + 16,
-                   // padded past a third of the SM's shared memory: at most two CTAs (2 x 256 TMEM columns) per SM
-                   EF_BYTES = 80 * 1024;
-static_assert(EF_SLOT + 16 <= EF_BYTES, "k_edges shared memory");
+// k_edges shared memory: the weight images once, then per pipeline an edge
+// feature tile, the hidden-activation tile, receiver/sender ids and an mbarrier.
+constexpr uint32_t EF_IMG1 = 0, EF_IMG2 = EF_IMG1 + kImg16, EF_B1 = EF_IMG2 + kImg128, EF_B2 = EF_B1 + 512,
+                   EF_BARS = EF_B2 + 512, EF_SLOT = EF_BARS + 32, EF_PIPE = (EF_SLOT + 16 + 1023) / 1024 * 1024,
+                   EF_P_XS = 0, EF_P_ZR = EF_P_XS + kImg16, EF_P_SR = EF_P_ZR + kImg128, EF_P_SJ = EF_P_SR + 512,
+                   EF_P_BYTES = EF_P_SJ + 512, EF_BYTES = EF_PIPE + 2 * EF_P_BYTES;
+static_assert(EF_PIPE % 1024 == 0 && EF_P_BYTES % 16 == 0, "k_edges shared memory alignment");
+static_assert(2 * EF_BYTES <= 227 * 1024, "two k_edges CTAs per SM");
 
+// Barrier of one 128-thread pipeline (named barrier 1 or 2, immediate ids).
+__device__ __forceinline__ void pipe_sync(int id) {
+    if (id == 1)
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+    else
+        asm volatile("bar.sync 2, 128;" ::: "memory");
+}
+__device__ __forceinline__ bool pipe_or(bool v, int id) {
+    uint32_t r;
+    if (id == 1)
+        asm volatile(
+            "{\n\t.reg .pred p, q;\n\t"
+            "setp.ne.u32 p, %1, 0;\n\t"
+            "bar.red.or.pred q, 1, 128, p;\n\t"
+            "selp.u32 %0, 1, 0, q;\n\t}"
+            : "=r"(r)
+            : "r"((uint32_t)v)
+            : "memory");
+    else
+        asm volatile(
+            "{\n\t.reg .pred p, q;\n\t"
+            "setp.ne.u32 p, %1, 0;\n\t"
+            "bar.red.or.pred q, 2, 128, p;\n\t"
+            "selp.u32 %0, 1, 0, q;\n\t}"
+            : "=r"(r)
+            : "r"((uint32_t)v)
+            : "memory");
+    return r != 0;
+}
+
+struct EdgeLoad {
+    int r, j;
+    float4 pr, pj, vr, vj;
+};
+
+// Edge ids of edge e (-1 past the end); positions and velocities follow in
+// edge_load_state, so the two dependent loads can be issued at different points.
+__device__ __forceinline__ void edge_load_ids(const EdgeArgs& a, int e, int E, EdgeLoad& L) {
+    L.r = -1;
+    L.j = -1;
+    if (e < E) {
+        L.r = __ldg(a.receiver + e);
+        L.j = __ldg(a.sender + e);
+    }
+}
+
+__device__ __forceinline__ void edge_load_state(const EdgeArgs& a, EdgeLoad& L) {
+    if (L.r >= 0) {
+        L.pr = __ldg(a.pos + L.r);
+        L.pj = __ldg(a.pos + L.j);
+        L.vr = __ldg(a.vel + L.r);
+        L.vj = __ldg(a.vel + L.j);
+    }
+}
+
+__device__ __forceinline__ uint4 edge_pack(const EdgeArgs& a, const EdgeLoad& L) {
+    if (L.r < 0) return make_uint4(0, 0, 0, 0);
+    const float dx = L.pj.x - L.pr.x, dy = L.pj.y - L.pr.y, dz = L.pj.z - L.pr.z;
+    const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
+    return make_uint4(pack2(dx * a.inv_r, dy * a.inv_r), pack2(dz * a.inv_r, dist * a.inv_r),
+                      pack2((L.vj.x - L.vr.x) * a.inv_vs, (L.vj.y - L.vr.y) * a.inv_vs),
+                      pack2((L.vj.z - L.vr.z) * a.inv_vs, 0.0f));
+}
+
+// Two independent pipelines of 4 warps per CTA (warps 0-3, 4-7), each owning
+// TMEM columns [128 p, 128 p + 128): layer 1 lands there (lane = edge), is
+// consumed by its epilogue, and layer 2 (lane = feature) overwrites it.  The
+// next tile's edge data are loaded while the current tile's epilogue runs.
 template <int MODE>
-__global__ void __launch_bounds__(kT) k_edges(EdgeArgs a) {
+__global__ void __launch_bounds__(2 * kT, 2) k_edges(EdgeArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* img1 = sm + EF_IMG1;
     uint8_t* img2 = sm + EF_IMG2;
-    uint8_t* xs = sm + EF_XS;
-    uint8_t* zr = sm + EF_ZR;
     float* b1 = reinterpret_cast<float*>(sm + EF_B1);
     float* b2 = reinterpret_cast<float*>(sm + EF_B2);
-    int* sr = reinterpret_cast<int*>(sm + EF_SR);
-    int* sj = reinterpret_cast<int*>(sm + EF_SJ);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + EF_BARS);
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + EF_BARS);  // [0],[1] pipelines, [2] bulk copy
     uint32_t* slot = reinterpret_cast<uint32_t*>(sm + EF_SLOT);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tid = threadIdx.x, warp = tid >> 5, p = warp >> 2, lt = tid & (kT - 1);
+    uint8_t* pb = sm + EF_PIPE + p * EF_P_BYTES;
+    uint8_t* xs = pb + EF_P_XS;
+    uint8_t* zr = pb + EF_P_ZR;
+    int* sr = reinterpret_cast<int*>(pb + EF_P_SR);
+    int* sj = reinterpret_cast<int*>(pb + EF_P_SJ);
+    uint64_t* bar = &bars[p];
+    const int bid = 1 + p;
     const int E = min(__ldg(a.offset + a.n_recv), a.cap);
 
-    const uint32_t tmem = cta_begin(bars, slot, 256);
-    b1[tid] = a.b1[tid];
-    b2[tid] = a.b2[tid];
     if (tid == 0) {
-        mbar_arrive_expect_tx(&bars[1], kImg16 + kImg128);
-        tma_load_1d(img1, a.img_e1, kImg16, &bars[1]);
-        tma_load_1d(img2, a.img_e2, kImg128, &bars[1]);
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        mbar_init(&bars[2], 1);
+        fence_mbar_init();
     }
-    bool failed = __syncthreads_or(!mbar_wait(&bars[1], 0, kPolls));
+    if (warp == 0) umma::tmem_alloc(slot, 256);
+    if (tid < 128) b1[tid] = a.b1[tid];
+    else b2[tid - 128] = a.b2[tid - 128];
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    const uint32_t tmem = *slot + 128u * p;
+    if (tid == 0) {
+        mbar_arrive_expect_tx(&bars[2], kImg16 + kImg128);
+        tma_load_1d(img1, a.img_e1, kImg16, &bars[2]);
+        tma_load_1d(img2, a.img_e2, kImg128, &bars[2]);
+    }
+    bool failed = __syncthreads_or(!mbar_wait(&bars[2], 0, kPolls));
     bool mine = true, pending = false;
     uint32_t phase = 0;
     constexpr uint32_t idesc = umma::idesc_bf16(128, 128);
-    const int c = tid;  // feature owned in the transposed epilogue
-    for (int tile = blockIdx.x; !failed && tile * kT < E; tile += gridDim.x) {
-        int r, j;
-        uint4 q0;
-        edge_features(a, tile * kT + tid, E, r, j, q0);
-        sr[tid] = r;
-        sj[tid] = j;
-        *reinterpret_cast<uint4*>(xs + tile_off(tid, 0, 16)) = q0;
-        *reinterpret_cast<uint4*>(xs + tile_off(tid, 8, 16)) = make_uint4(0, 0, 0, 0);
-        operands_ready();
-        if (tid == 0) {
+    const int stride = 2 * gridDim.x;
+    int tile = 2 * blockIdx.x + p;
+    EdgeLoad nxt;
+    edge_load_ids(a, tile * kT + lt, E, nxt);
+    edge_load_state(a, nxt);
+    for (; !failed && tile * kT < E; tile += stride) {
+        const EdgeLoad cur_e = nxt;
+        sr[lt] = cur_e.r;
+        sj[lt] = cur_e.j;
+        *reinterpret_cast<uint4*>(xs + tile_off(lt, 0, 16)) = edge_pack(a, cur_e);
+        *reinterpret_cast<uint4*>(xs + tile_off(lt, 8, 16)) = make_uint4(0, 0, 0, 0);
+        fence_proxy_async_smem();
+        umma::fence_before();
+        pipe_sync(bid);
+        if (lt == 0) {
             umma::fence_after();
-            umma::mma_tile(tmem, xs, img1, 16, idesc, false);  // D1[e][k]
-            umma::commit(&bars[0]);
+            umma::mma_tile(tmem, xs, img1, 16, idesc, false);  // D[e][k]
+            umma::commit(bar);
         }
+        edge_load_ids(a, (tile + stride) * kT + lt, E, nxt);  // prefetch the next tile's ids
         pending = true;
-        if (!mma_done(bars, phase, mine)) { failed = true; break; }
+        mine = mbar_wait(bar, phase, kPolls);
+        if (pipe_or(!mine, bid)) { failed = true; break; }
+        phase ^= 1u;
         pending = false;
-        // layer-1 epilogue: row = edge tid
+        umma::fence_after();
 #pragma unroll
         for (int c0 = 0; c0 < 128; c0 += 32) {
             float v[32];
-            umma::tmem_ld32(umma::taddr(tmem, 32 * warp, c0), v);
+            umma::tmem_ld32(umma::taddr(tmem, 32 * (warp & 3), c0), v);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int k = c0 + 8 * q;
@@ -359,33 +451,51 @@ __global__ void __launch_bounds__(kT) k_edges(EdgeArgs a) {
                 w.y = pack2(fmaxf(v[8 * q + 2] + b1[k + 2], 0.f), fmaxf(v[8 * q + 3] + b1[k + 3], 0.f));
                 w.z = pack2(fmaxf(v[8 * q + 4] + b1[k + 4], 0.f), fmaxf(v[8 * q + 5] + b1[k + 5], 0.f));
                 w.w = pack2(fmaxf(v[8 * q + 6] + b1[k + 6], 0.f), fmaxf(v[8 * q + 7] + b1[k + 7], 0.f));
-                *reinterpret_cast<uint4*>(zr + tile_off(tid, k, 128)) = w;
+                *reinterpret_cast<uint4*>(zr + tile_off(lt, k, 128)) = w;
             }
         }
-        operands_ready();
-        if (tid == 0) {
+        fence_proxy_async_smem();
+        umma::fence_before();
+        pipe_sync(bid);
+        if (lt == 0) {
             umma::fence_after();
-            umma::mma_tile(tmem + 128, img2, zr, 128, idesc, false);  // D2[c][e]
-            umma::commit(&bars[0]);
+            umma::mma_tile(tmem, img2, zr, 128, idesc, false);  // D[c][e], over layer 1's columns
+            umma::commit(bar);
         }
+        edge_load_state(a, nxt);  // and its particle state
         pending = true;
-        if (!mma_done(bars, phase, mine)) { failed = true; break; }
+        mine = mbar_wait(bar, phase, kPolls);
+        if (pipe_or(!mine, bid)) { failed = true; break; }
+        phase ^= 1u;
         pending = false;
-        // layer-2 epilogue: lane = feature c, columns = edges of the tile
+        umma::fence_after();
+        // layer-2 epilogue: lane = feature c, columns = the tile's edges
+        const int c = lt;
         const float bc = b2[c];
         int cur = -1;
         float acc = 0.0f, gval = 0.0f;
-#pragma unroll 1
-        for (int c0 = 0; c0 < 128; c0 += 32) {
-            float v[32];
-            umma::tmem_ld32(umma::taddr(tmem + 128, 32 * warp, c0), v);
-            if (MODE == MODE_AGG) {
-                float hv[32];
+        if (MODE == MODE_AGG) {
+            // gathers of the next 32 edges are in flight while these 32 are summed
+            uint16_t hn[32];
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int jj = sj[c0 + i];
-                    hv[i] = jj >= 0 ? bf(__ldg(a.h + (size_t)jj * kH + c)) : 0.0f;
+            for (int i = 0; i < 32; ++i) {
+                const int jj = sj[i];
+                hn[i] = jj >= 0 ? __ldg(a.h + (size_t)jj * kH + c) : (uint16_t)0;
+            }
+#pragma unroll
+            for (int c0 = 0; c0 < 128; c0 += 32) {
+                uint16_t hv[32];
+#pragma unroll
+                for (int i = 0; i < 32; ++i) hv[i] = hn[i];
+                if (c0 + 32 < 128) {
+#pragma unroll
+                    for (int i = 0; i < 32; ++i) {
+                        const int jj = sj[c0 + 32 + i];
+                        hn[i] = jj >= 0 ? __ldg(a.h + (size_t)jj * kH + c) : (uint16_t)0;
+                    }
                 }
+                float v[32];
+                umma::tmem_ld32(umma::taddr(tmem, 32 * (warp & 3), c0), v);
 #pragma unroll
                 for (int i = 0; i < 32; ++i) {
                     const int rr = sr[c0 + i];
@@ -395,9 +505,14 @@ __global__ void __launch_bounds__(kT) k_edges(EdgeArgs a) {
                         cur = rr;
                         acc = 0.0f;
                     }
-                    acc = fmaf(v[i] + bc, hv[i], acc);
+                    acc = fmaf(v[i] + bc, bf(hv[i]), acc);
                 }
-            } else {
+            }
+        } else {
+#pragma unroll 1
+            for (int c0 = 0; c0 < 128; c0 += 32) {
+                float v[32];
+                umma::tmem_ld32(umma::taddr(tmem, 32 * (warp & 3), c0), v);
 #pragma unroll 4
                 for (int i = 0; i < 32; ++i) {
                     const int rr = sr[c0 + i];
@@ -412,9 +527,16 @@ __global__ void __launch_bounds__(kT) k_edges(EdgeArgs a) {
         }
         if (MODE == MODE_AGG && cur >= 0) atomicAdd(a.agg + (size_t)cur * kH + c, acc * a.inv_norm);
         umma::fence_before();
-        __syncthreads();
+        pipe_sync(bid);
     }
-    cta_end(bars, phase, pending && !mine, tmem, 256, a.status, failed);
+    if (failed && lt == 0) raise_flag(a.status, SPHDEM_FLAG_TIMEOUT);
+    if (pending && !mine) mbar_wait(bar, phase, kPolls);
+    umma::fence_before();
+    __syncthreads();
+    if (warp == 0) {
+        umma::fence_after();
+        umma::tmem_dealloc(*slot, 256);
+    }
 }
 
 // k_edges_bwd shared memory
@@ -827,11 +949,11 @@ __global__ void k_apply(ApplyArgs a) {
     }
 }
 
-__global__ void k_maxdev(const float* __restrict__ a, const float* __restrict__ b, int n, float inv,
+__global__ void k_maxdev(const float* __restrict__ a, const float* __restrict__ b, float ref, int n, float inv,
                          float* __restrict__ out) {
     float m = 0.0f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-        m = fmaxf(m, fabsf(a[i] - b[i]) * inv);
+        m = fmaxf(m, fabsf(a[i] - (b ? b[i] : ref)) * inv);
     for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
     if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(reinterpret_cast<int*>(out), __float_as_int(m));
 }
@@ -886,31 +1008,47 @@ __global__ void k_nodes(sphdem_mpnn_nodes_t a) {
     o[1] = make_uint4(pack2(f[8], f[9]), pack2(f[10], f[11]), pack2(f[12], f[13]), pack2(f[14], f[15]));
 }
 
+// One warp per receiver: the lanes test 32 candidate slots at a time (ranges
+// of the ball-trimmed cell columns, in column order); accepted senders are
+// compacted in slot order by ballot, so the list is deterministic.
 template <bool FILL>
 __global__ void k_graph(Geo g, const float4* __restrict__ pos, int n_recv, float r2, float rq, int* __restrict__ offset,
                         int* __restrict__ sender, int* __restrict__ receiver, int cap, sphdem_ctl_t* ctl) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_recv) return;
+    const int i = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= n_recv) return;  // warp-uniform
     const float4 p = __ldg(pos + i);
     const int inst = inst_of(g, i);
     const int base = FILL ? offset[i] : 0;
+    const unsigned below = (1u << lane) - 1u;
     int cnt = 0;
-    for_each_range_ball(g, p.x, p.y, p.z, rq, inst, [&](int s, int e) {
-        for (int k = s; k < e; ++k) {
-            const int j = __ldg(g.order + k);
-            if (j == i) continue;
-            const float4 q = __ldg(pos + j);
-            if (d2_exact(p.x, p.y, p.z, q.x, q.y, q.z).d2 < r2) {
-                if (FILL && base + cnt < cap) {
-                    sender[base + cnt] = j;
-                    receiver[base + cnt] = i;
+    warp_ranges_ball(g, p.x, p.y, p.z, rq, inst, [&](int s, int e) {
+        for (int k0 = s; k0 < e; k0 += 32) {
+            const int k = k0 + lane;
+            bool in = false;
+            int j = -1;
+            if (k < e) {
+                j = __ldg(g.order + k);
+                if (j != i) {
+                    const float4 q = __ldg(pos + j);
+                    in = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z).d2 < r2;
                 }
-                ++cnt;
             }
+            const unsigned m = __ballot_sync(0xffffffffu, in);
+            if (FILL && in) {
+                const int slot = base + cnt + __popc(m & below);
+                if (slot < cap) {
+                    sender[slot] = j;
+                    receiver[slot] = i;
+                }
+            }
+            cnt += __popc(m);
         }
     });
-    if (!FILL) offset[i] = cnt;
-    else if (i == n_recv - 1 && base + cnt > cap) flag(ctl, SPHDEM_FLAG_ROW_OVERFLOW);
+    if (lane == 0) {
+        if (!FILL) offset[i] = cnt;
+        else if (i == n_recv - 1 && base + cnt > cap) flag(ctl, SPHDEM_FLAG_ROW_OVERFLOW);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1027,7 +1165,7 @@ template <int MODE>
 int edges(const EdgeArgs& a, int grid, cudaStream_t st) {
     int rc = smem_opt_in(k_edges<MODE>, EF_BYTES);
     if (rc) return rc;
-    k_edges<MODE><<<grid, kT, EF_BYTES, st>>>(a);
+    k_edges<MODE><<<grid, 2 * kT, EF_BYTES, st>>>(a);
     return launch_status("mpnn edges");
 }
 
@@ -1088,12 +1226,11 @@ extern "C" int sphdem_mpnn_graph(sphdem_grid_t* grid, const float* node_pos3, co
     const float r2 = radius * radius;
     const float rq = pad_radius(radius);
     const float4* p4 = reinterpret_cast<const float4*>(node_pos4);
-    k_graph<false><<<blocks_for(n_recv, 128), 128, 0, st>>>(g, p4, n_recv, r2, rq, offset, sender, receiver,
-                                                            edge_capacity, ctl);
+    const int nb = blocks_for((long)n_recv * 32, 256);
+    k_graph<false><<<nb, 256, 0, st>>>(g, p4, n_recv, r2, rq, offset, sender, receiver, edge_capacity, ctl);
     rc = scan_counts(offset, n_recv, scan_scratch, st);
     if (rc) return rc;
-    k_graph<true><<<blocks_for(n_recv, 128), 128, 0, st>>>(g, p4, n_recv, r2, rq, offset, sender, receiver,
-                                                           edge_capacity, ctl);
+    k_graph<true><<<nb, 256, 0, st>>>(g, p4, n_recv, r2, rq, offset, sender, receiver, edge_capacity, ctl);
     return launch_status("mpnn_graph");
 }
 
@@ -1264,16 +1401,16 @@ extern "C" int sphdem_mpnn_apply(float* f_pos, float* f_vel, const float* f_acc,
     return launch_status("mpnn_apply");
 }
 
-extern "C" int sphdem_mpnn_maxdev(const float* a, const float* b, int32_t n, float inv, float* out,
+extern "C" int sphdem_mpnn_maxdev(const float* a, const float* b, float ref, int32_t n, float inv, float* out,
                                   sphdem_stream_t stream) {
-    if (!a || !b || !out || n < 0) {
+    if (!a || !out || n < 0) {
         set_error_msg("mpnn_maxdev: invalid arguments");
         return SPHDEM_ERR_INVALID;
     }
     if (n == 0) return SPHDEM_OK;
     int grid = blocks_for(n, 256);
     if (grid > 4 * sm_count()) grid = 4 * sm_count();
-    k_maxdev<<<grid, 256, 0, as_stream(stream)>>>(a, b, n, inv, out);
+    k_maxdev<<<grid, 256, 0, as_stream(stream)>>>(a, b, ref, n, inv, out);
     return launch_status("mpnn_maxdev");
 }
 

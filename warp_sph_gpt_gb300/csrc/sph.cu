@@ -1,6 +1,7 @@
 // sph.cu -- WCSPH neighbour loops on the sorted fluid / wall copies.
 //
-// One thread per subject, subjects taken in cell order (grid order), so the
+// One thread per subject (or, for small systems, one warp per subject: the
+// launch option lanes = 32), subjects taken in cell order (grid order), so the
 // threads of a warp query the same few cell columns and their float4
 // neighbour loads hit the same L1 lines.  Neighbour membership uses the exact
 // FP32 predicates of the reference; the physics sums use contracted FP32.
@@ -21,6 +22,37 @@ namespace sd {
 
 namespace {
 
+// Subject of this thread (LANES = 1) or of this warp (LANES = 32), and the
+// neighbour visitor: a thread walks every slot of the ball-trimmed ranges; a
+// warp takes the ranges together and its lanes stride through each one.  The
+// warp form has 32x the parallelism for small systems; its sums are reduced
+// across lanes at the end (a different, equally valid FP32 summation order).
+template <int LANES>
+__device__ __forceinline__ int subject_index(int& lane) {
+    const long t = blockIdx.x * (long)blockDim.x + threadIdx.x;
+    lane = LANES == 1 ? 0 : (int)(threadIdx.x & 31);
+    return (int)(LANES == 1 ? t : t >> 5);
+}
+
+template <int LANES, class F>
+__device__ __forceinline__ void visit_ball(const Geo& g, float px, float py, float pz, float rq, int inst, int lane,
+                                           F&& body) {
+    if (LANES == 1) {
+        for_each_range_ball(g, px, py, pz, rq, inst, [&](int s, int e) {
+            for (int j = s; j < e; ++j) body(j);
+        });
+    } else {
+        warp_ranges_ball(g, px, py, pz, rq, inst, [&](int s, int e) {
+            for (int j = s + lane; j < e; j += 32) body(j);
+        });
+    }
+}
+
+template <int LANES>
+__device__ __forceinline__ float lanes_sum(float v) {
+    return LANES == 1 ? v : warp_sum(v);
+}
+
 struct DensArgs {
     Geo gs, gb;
     const float4* __restrict__ f_posm;
@@ -38,38 +70,38 @@ struct DensArgs {
     float rho0, B, gamma;
 };
 
-template <bool FLT, bool RHO, bool PRES>
+template <int LANES, bool FLT, bool RHO, bool PRES>
 __global__ void __launch_bounds__(256) k_density(DensArgs a) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane;
+    const int k = subject_index<LANES>(lane);
     if (k >= a.n) return;
     const int o = a.gs.order[k];
     const float4 p = a.f_posm[k];
     const int inst = inst_of(a.gs, o);
     float rho_sum = 0.0f, flt_sum = 0.0f;
-    for_each_range_ball(a.gs, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
-        for (int j = s; j < e; ++j) {
-            const float4 q = a.f_posm[j];
+    visit_ball<LANES>(a.gs, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+        const float4 q = a.f_posm[j];
+        const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+        if (r.d2 < a.s2) {
+            const float w = kern_w(a.kern, fast_sqrt(r.d2));
+            if (RHO) rho_sum += q.w * w;
+            if (FLT) flt_sum += a.f_vprev[j] * w;
+        }
+    });
+    if (a.gb.ncl > 0) {
+        visit_ball<LANES>(a.gb, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+            const float4 q = a.b_posm[j];
             const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
             if (r.d2 < a.s2) {
                 const float w = kern_w(a.kern, fast_sqrt(r.d2));
                 if (RHO) rho_sum += q.w * w;
-                if (FLT) flt_sum += a.f_vprev[j] * w;
-            }
-        }
-    });
-    if (a.gb.ncl > 0) {
-        for_each_range_ball(a.gb, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
-            for (int j = s; j < e; ++j) {
-                const float4 q = a.b_posm[j];
-                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-                if (r.d2 < a.s2) {
-                    const float w = kern_w(a.kern, fast_sqrt(r.d2));
-                    if (RHO) rho_sum += q.w * w;
-                    if (FLT) flt_sum += a.b_vprev[j] * w;
-                }
+                if (FLT) flt_sum += a.b_vprev[j] * w;
             }
         });
     }
+    if (RHO) rho_sum = lanes_sum<LANES>(rho_sum);
+    if (FLT) flt_sum = lanes_sum<LANES>(flt_sum);
+    if (lane != 0) return;
     if (FLT) a.flt[o] = flt_sum;
     if (RHO) {
         const float flt = FLT ? flt_sum : a.flt[o];
@@ -99,23 +131,24 @@ struct WallArgs {
     float rho0, B, gamma;
 };
 
-template <bool PRES>
+template <int LANES, bool PRES>
 __global__ void __launch_bounds__(256) k_density_wall(WallArgs a) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane;
+    const int k = subject_index<LANES>(lane);
     if (k >= a.n) return;
     const int o = a.gb.order[k];
     const float4 p = a.b_posm[k];
     const int inst = inst_of(a.gb, o);
     float rho_sum = 0.0f;
     if (a.gs.ncl > 0) {
-        for_each_range_ball(a.gs, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
-            for (int j = s; j < e; ++j) {
-                const float4 q = a.f_posm[j];
-                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-                if (r.d2 < a.s2) rho_sum += q.w * kern_w(a.kern, fast_sqrt(r.d2));
-            }
+        visit_ball<LANES>(a.gs, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+            const float4 q = a.f_posm[j];
+            const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+            if (r.d2 < a.s2) rho_sum += q.w * kern_w(a.kern, fast_sqrt(r.d2));
         });
     }
+    rho_sum = lanes_sum<LANES>(rho_sum);
+    if (lane != 0) return;
     const float rho = rho_sum + a.b_self[k];
     a.rho[o] = rho;
     if (PRES) {
@@ -171,9 +204,10 @@ __device__ __forceinline__ void force_pair(const ForceArgs& a, const D2& r, cons
     }
 }
 
-template <int MODE>
+template <int LANES, int MODE>
 __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    int lane;
+    const int k = subject_index<LANES>(lane);
     if (k >= a.n) return;
     const int o = a.gs.order[k];
     const float4 p = a.f_posm[k];
@@ -181,24 +215,31 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
     const float4 rpi = a.f_rp[k];
     const int inst = inst_of(a.gs, o);
     float3 acc = make_float3(0.f, 0.f, 0.f), pgf = make_float3(0.f, 0.f, 0.f);
-    for_each_range_ball(a.gs, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
-        for (int j = s; j < e; ++j) {
-            const float4 q = a.f_posm[j];
-            const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-            if (r.d2 > kR2Min && r.d2 < a.s2)
-                force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.f_rp[j], a.f_vel, j, acc, pgf);
-        }
+    visit_ball<LANES>(a.gs, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+        const float4 q = a.f_posm[j];
+        const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+        if (r.d2 > kR2Min && r.d2 < a.s2)
+            force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.f_rp[j], a.f_vel, j, acc, pgf);
     });
     if (a.gb.ncl > 0) {
-        for_each_range_ball(a.gb, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
-            for (int j = s; j < e; ++j) {
-                const float4 q = a.b_posm[j];
-                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-                if (r.d2 > kR2Min && r.d2 < a.s2)
-                    force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.b_rp[j], a.b_vel, j, acc, pgf);
-            }
+        visit_ball<LANES>(a.gb, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+            const float4 q = a.b_posm[j];
+            const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+            if (r.d2 > kR2Min && r.d2 < a.s2)
+                force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.b_rp[j], a.b_vel, j, acc, pgf);
         });
     }
+    if (MODE & 1) {
+        acc.x = lanes_sum<LANES>(acc.x);
+        acc.y = lanes_sum<LANES>(acc.y);
+        acc.z = lanes_sum<LANES>(acc.z);
+    }
+    if (MODE & 2) {
+        pgf.x = lanes_sum<LANES>(pgf.x);
+        pgf.y = lanes_sum<LANES>(pgf.y);
+        pgf.z = lanes_sum<LANES>(pgf.z);
+    }
+    if (lane != 0) return;
     if (MODE & 1) st3(a.acc, o, make_float3(acc.x, acc.y, acc.z - a.g));
     if (MODE & 2) {
         if (a.pgf) st3(a.pgf, o, pgf);
@@ -227,7 +268,7 @@ static float tait_B(float rho0, float c0, float gamma) { return rho0 * c0 * c0 /
 static int launch_block(int b) { return (b == 64 || b == 256) ? b : 128; }
 
 int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
-                float gamma, cudaStream_t st, int block) {
+                float gamma, cudaStream_t st, int block, int lanes) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     DensArgs a;
@@ -250,22 +291,37 @@ int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rh
     a.rho0 = rho0;
     a.B = tait_B(rho0, c0, gamma);
     a.gamma = gamma;
-    const int bs = launch_block(block), nb = blocks_for(n, bs);
-    if (flt && rho && pres)
-        k_density<true, true, true><<<nb, bs, 0, st>>>(a);
-    else if (!flt && rho && pres)
-        k_density<false, true, true><<<nb, bs, 0, st>>>(a);
-    else if (flt && !rho)
-        k_density<true, false, false><<<nb, bs, 0, st>>>(a);
-    else if (!flt && rho && !pres)
-        k_density<false, true, false><<<nb, bs, 0, st>>>(a);
-    else
-        k_density<true, true, false><<<nb, bs, 0, st>>>(a);
+    const int bs = launch_block(block);
+    if (lanes == 32) {
+        const int nb = blocks_for((long)n * 32, bs);
+        if (flt && rho && pres)
+            k_density<32, true, true, true><<<nb, bs, 0, st>>>(a);
+        else if (!flt && rho && pres)
+            k_density<32, false, true, true><<<nb, bs, 0, st>>>(a);
+        else if (flt && !rho)
+            k_density<32, true, false, false><<<nb, bs, 0, st>>>(a);
+        else if (!flt && rho && !pres)
+            k_density<32, false, true, false><<<nb, bs, 0, st>>>(a);
+        else
+            k_density<32, true, true, false><<<nb, bs, 0, st>>>(a);
+    } else {
+        const int nb = blocks_for(n, bs);
+        if (flt && rho && pres)
+            k_density<1, true, true, true><<<nb, bs, 0, st>>>(a);
+        else if (!flt && rho && pres)
+            k_density<1, false, true, true><<<nb, bs, 0, st>>>(a);
+        else if (flt && !rho)
+            k_density<1, true, false, false><<<nb, bs, 0, st>>>(a);
+        else if (!flt && rho && !pres)
+            k_density<1, false, true, false><<<nb, bs, 0, st>>>(a);
+        else
+            k_density<1, true, true, false><<<nb, bs, 0, st>>>(a);
+    }
     return launch_status("density");
 }
 
 int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, float rho0, float c0, float gamma,
-                     cudaStream_t st, int block) {
+                     cudaStream_t st, int block, int lanes) {
     const int n = c->bnd.n;
     if (n <= 0) return SPHDEM_OK;
     WallArgs a;
@@ -286,14 +342,23 @@ int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, f
     a.B = tait_B(rho0, c0, gamma);
     a.gamma = gamma;
     const int bs = launch_block(block);
-    if (pres)
-        k_density_wall<true><<<blocks_for(n, bs), bs, 0, st>>>(a);
-    else
-        k_density_wall<false><<<blocks_for(n, bs), bs, 0, st>>>(a);
+    if (lanes == 32) {
+        const int nb = blocks_for((long)n * 32, bs);
+        if (pres)
+            k_density_wall<32, true><<<nb, bs, 0, st>>>(a);
+        else
+            k_density_wall<32, false><<<nb, bs, 0, st>>>(a);
+    } else {
+        if (pres)
+            k_density_wall<1, true><<<blocks_for(n, bs), bs, 0, st>>>(a);
+        else
+            k_density_wall<1, false><<<blocks_for(n, bs), bs, 0, st>>>(a);
+    }
     return launch_status("density_wall");
 }
 
-int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st, int block) {
+int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st, int block,
+              int lanes) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     ForceArgs a;
@@ -316,13 +381,24 @@ int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, 
     a.two_mu = 2.0f * mu;
     a.eps_h2 = 0.01f * h * h;
     a.g = g;
-    const int bs = launch_block(block), nb = blocks_for(n, bs);
-    if (mode == 3)
-        k_force<3><<<nb, bs, 0, st>>>(a);
-    else if (mode == 2)
-        k_force<2><<<nb, bs, 0, st>>>(a);
-    else
-        k_force<1><<<nb, bs, 0, st>>>(a);
+    const int bs = launch_block(block);
+    if (lanes == 32) {
+        const int nb = blocks_for((long)n * 32, bs);
+        if (mode == 3)
+            k_force<32, 3><<<nb, bs, 0, st>>>(a);
+        else if (mode == 2)
+            k_force<32, 2><<<nb, bs, 0, st>>>(a);
+        else
+            k_force<32, 1><<<nb, bs, 0, st>>>(a);
+    } else {
+        const int nb = blocks_for(n, bs);
+        if (mode == 3)
+            k_force<1, 3><<<nb, bs, 0, st>>>(a);
+        else if (mode == 2)
+            k_force<1, 2><<<nb, bs, 0, st>>>(a);
+        else
+            k_force<1, 1><<<nb, bs, 0, st>>>(a);
+    }
     return launch_status("force");
 }
 

@@ -26,11 +26,11 @@ int gather_fluid(const sphdem_ctx_t* c, cudaStream_t st);
 int gather_wall(const sphdem_ctx_t* c, float support, float h, cudaStream_t st);
 int gather_wall_rho(const sphdem_ctx_t* c, cudaStream_t st);
 int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
-                float gamma, cudaStream_t st, int block = 0);
+                float gamma, cudaStream_t st, int block = 0, int lanes = 1);
 int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, float rho0, float c0, float gamma,
-                     cudaStream_t st, int block = 0);
+                     cudaStream_t st, int block = 0, int lanes = 1);
 int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st,
-              int block = 0);
+              int block = 0, int lanes = 1);
 int run_pres(const float* rho, float* pres, int n, float rho0, float c0, float gamma, cudaStream_t st);
 int run_step_sph(const sphdem_ctx_t* c, float dt, cudaStream_t st);
 int run_contacts(const sphdem_ctx_t* c, float radius_max, float bnd_radius_max, float g, float dt, int which,
@@ -79,11 +79,11 @@ bool shepard_due(const sphdem_params_t* p, int step) {
 // write_pgf; the acceleration arithmetic is the same either way.
 int sph_part(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool write_pgf, cudaStream_t st) {
     if (shep) TRY(gather_wall_rho(c, st));
-    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph));
-    TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph));
+    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
+    TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
     sphdem_ctx_t cc = *c;
     if (!write_pgf) cc.sph.pgf = nullptr;
-    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph);
+    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph);
 }
 
 int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integrate, cudaStream_t st) {
@@ -392,7 +392,7 @@ int sphdem_struct_sizes(int64_t* out, int n) {
                          (int64_t)sizeof(sphdem_ctl_t),   (int64_t)sizeof(sphdem_work_t),
                          (int64_t)sizeof(sphdem_params_t), (int64_t)sizeof(sphdem_ctx_t),
                          (int64_t)sizeof(sphdem_mpnn_nodes_t), (int64_t)sizeof(sphdem_mpnn_net_t),
-                         (int64_t)sizeof(sphdem_mpnn_grad_t)};
+                         (int64_t)sizeof(sphdem_mpnn_grad_t), (int64_t)sizeof(sphdem_jump_t)};
     const int m = (int)(sizeof(s) / sizeof(s[0]));
     for (int i = 0; i < n && i < m; ++i) out[i] = s[i];
     return m;
@@ -475,6 +475,142 @@ int sphdem_run(sphdem_ctx_t* c, const sphdem_params_t* p, int first_step, int n_
     return SPHDEM_OK;
 }
 
+// ---------------------------------------------------------------------------
+// learned jump (include/sphdem_mpnn.h)
+// ---------------------------------------------------------------------------
+namespace {
+
+int copy_d2d(float* dst, const float* src, size_t n, cudaStream_t st) {
+    if (n == 0) return SPHDEM_OK;
+    cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) {
+        set_error("jump copy", e);
+        return SPHDEM_ERR_CUDA;
+    }
+    return SPHDEM_OK;
+}
+
+int jump_keep(sphdem_ctx_t* c, const sphdem_jump_t* j, bool restore, cudaStream_t st) {
+    const size_t nf = (size_t)c->sph.n, nd = (size_t)c->dem.n;
+    float* k = j->keep;
+    float* live[5] = {c->sph.pos, c->sph.vel, c->dem.pos, c->dem.vel, c->sph.rho};
+    const size_t len[5] = {3 * nf, 3 * nf, 3 * nd, 3 * nd, nf};
+    for (int i = 0; i < 5; ++i) {
+        TRY(restore ? copy_d2d(live[i], k, len[i], st) : copy_d2d(k, live[i], len[i], st));
+        k += len[i];
+    }
+    return SPHDEM_OK;
+}
+
+int jump_body(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, bool shep, cudaStream_t st) {
+    TRY(loop_body(c, p, shep, 1, st));
+    TRY(jump_keep(c, j, false, st));
+    TRY(sphdem_mpnn_nodes(&j->nodes, st));
+    sphdem_grid_t g = j->node_grid;
+    TRY(sphdem_mpnn_graph(&g, j->nodes.node_pos3, j->nodes.node_pos4, j->net.n_recv, j->radius, j->net.offset,
+                          j->net.sender, j->net.receiver, j->net.edge_capacity, j->scan_scratch, j->graph_ctl, st));
+    TRY(sphdem_mpnn_forward(&j->net, 0, st));
+    TRY(sphdem_mpnn_apply(c->sph.pos, c->sph.vel, c->sph.acc, c->sph.n, c->dem.pos, c->dem.vel, c->dem.acc,
+                          c->dem.n, j->net.out, j->substeps, p->dt, j->scale, nullptr, nullptr, nullptr, st));
+    TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
+    TRY(gather_fluid(c, st));
+    TRY(run_density(c, p->support, p->h, false, true, false, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
+    cudaError_t e = cudaMemsetAsync(j->dev, 0, sizeof(float), st);
+    if (e != cudaSuccess) {
+        set_error("jump", e);
+        return SPHDEM_ERR_CUDA;
+    }
+    const float* rho_old = j->keep + 6 * (size_t)c->sph.n + 6 * (size_t)c->dem.n;
+    return sphdem_mpnn_maxdev(c->sph.rho, j->judge == 1 ? nullptr : rho_old, p->rho0, c->sph.n, 1.0f / p->rho0,
+                              j->dev, st);
+}
+
+struct JumpEntry {
+    sphdem_ctx_t snap;
+    sphdem_params_t params;
+    sphdem_jump_t jump;
+    cudaStream_t cap = nullptr;
+    cudaGraphExec_t exec[2] = {nullptr, nullptr};
+    bool warm[2] = {false, false};
+};
+std::map<const sphdem_ctx_t*, JumpEntry> g_jumps;
+
+}  // namespace
+
+int sphdem_jump(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, int step, sphdem_stream_t stream) {
+    if (!valid_ctx(c) || !p || !j || !j->keep || !j->dev || !j->graph_ctl || !j->scan_scratch || j->substeps < 1 ||
+        c->dem.n < 0) {
+        set_error_msg("jump: invalid arguments");
+        return SPHDEM_ERR_INVALID;
+    }
+    cudaStream_t st = as_stream(stream);
+    const bool shep = shepard_due(p, step);
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    JumpEntry& e = g_jumps[c];
+    if (memcmp(&e.snap, c, sizeof(*c)) != 0 || memcmp(&e.params, p, sizeof(*p)) != 0 ||
+        memcmp(&e.jump, j, sizeof(*j)) != 0) {
+        for (auto& x : e.exec)
+            if (x) {
+                cudaGraphExecDestroy(x);
+                x = nullptr;
+            }
+        e.warm[0] = e.warm[1] = false;
+        e.snap = *c;
+        e.params = *p;
+        e.jump = *j;
+    }
+    const int v = shep ? 1 : 0;
+    if (!e.warm[v]) {  // first use runs eagerly (one-time kernel attribute set-up), later ones replay
+        e.warm[v] = true;
+        return jump_body(c, p, j, shep, st);
+    }
+    if (!e.cap) {
+        cudaError_t err = cudaStreamCreateWithFlags(&e.cap, cudaStreamNonBlocking);
+        if (err != cudaSuccess) {
+            set_error("jump capture stream", err);
+            return SPHDEM_ERR_CUDA;
+        }
+    }
+    if (!e.exec[v]) {
+        cudaError_t err = cudaStreamBeginCapture(e.cap, cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) {
+            set_error("jump capture begin", err);
+            return SPHDEM_ERR_CUDA;
+        }
+        int rc = jump_body(c, p, j, shep, e.cap);
+        cudaGraph_t graph = nullptr;
+        err = cudaStreamEndCapture(e.cap, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        if (err != cudaSuccess) {
+            set_error("jump capture end", err);
+            return SPHDEM_ERR_CUDA;
+        }
+        err = cudaGraphInstantiate(&e.exec[v], graph, 0);
+        cudaGraphDestroy(graph);
+        if (err != cudaSuccess) {
+            set_error("jump graph instantiate", err);
+            return SPHDEM_ERR_CUDA;
+        }
+    }
+    cudaError_t err = cudaGraphLaunch(e.exec[v], st);
+    if (err != cudaSuccess) {
+        set_error("jump graph launch", err);
+        return SPHDEM_ERR_CUDA;
+    }
+    return SPHDEM_OK;
+}
+
+int sphdem_jump_undo(sphdem_ctx_t* c, const sphdem_jump_t* j, sphdem_stream_t stream) {
+    if (!valid_ctx(c) || !j || !j->keep) {
+        set_error_msg("jump_undo: invalid arguments");
+        return SPHDEM_ERR_INVALID;
+    }
+    return jump_keep(c, j, true, as_stream(stream));
+}
+
 // Blocking helper: one loop body of run_forward (moving-grid rebuild + one
 // step) with a CUDA event between phases on the launch stream; fills ms[k]
 // with the duration of phase k (SPHDEM_PHASE_* order) and synchronises.
@@ -496,13 +632,13 @@ int sphdem_profile_step(sphdem_ctx_t* c, const sphdem_params_t* p, int step, int
         if (coupled && (rc = build_grid(&c->grid_dem, c->dem.pos, c->ctl, st))) break;
         mark();
         if (shep && (rc = gather_wall_rho(c, st))) break;
-        if ((rc = run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph))) break;
+        if ((rc = run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph))) break;
         mark();
-        if ((rc = run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph))) break;
+        if ((rc = run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph))) break;
         mark();
         sphdem_ctx_t cc = *c;
         if (!coupled) cc.sph.pgf = nullptr;
-        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph))) break;
+        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph))) break;
         mark();
         if (coupled && (rc = run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, st))) break;
         mark();

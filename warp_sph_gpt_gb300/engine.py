@@ -48,7 +48,7 @@ class StepContext:
         self._status_host = torch.zeros(16, dtype=torch.int32, pin_memory=True)
         self._status_event = None
         # launch tuning (results do not depend on it): see autotune.py
-        self.tuning = {"block_sph": 0, "porosity_variant": 0}
+        self.tuning = {"block_sph": 0, "porosity_variant": 0, "lanes_sph": 1}
         self._alloc_work()
         addr = C.addressof(self.ctx)
         weakref.finalize(self, _release, self.lib, addr)
@@ -164,6 +164,7 @@ class StepContext:
             p.radius_max, p.boundary_radius_max, p.h_max, p.h_uniform = (float(x) for x in scales)
         p.block_sph = int(self.tuning.get("block_sph", 0))
         p.porosity_variant = int(self.tuning.get("porosity_variant", 0))
+        p.lanes_sph = int(self.tuning.get("lanes_sph", 1))
 
     @property
     def stream(self):

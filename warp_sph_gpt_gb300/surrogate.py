@@ -11,8 +11,9 @@ current one.  One *jump* of K = m + 1 steps is
        x += m dt v + dt^2 a_s m(m+1)/2,  v += m dt a_s
      (the prior is what m symplectic-Euler substeps give if a_s stays fixed);
   3. the judge: the plain density kernel evaluated at the new positions.  If
-     any fluid density moved by more than ``tol * rho0`` from its value at the
-     start of the jump, the jump is undone and m plain steps run instead.
+     the density deviation max_i |rho_i - rho0| / rho0 exceeds ``tol`` (or,
+     with judge = 0, any density moved by more than tol * rho0 over the
+     jump), the jump is undone and m plain steps run instead.
 
 The plain step is therefore both the fallback and the judge of the density
 error.  The network is trained on trajectories of the batched plain solver
@@ -52,7 +53,8 @@ class SurrogateConfig:
     a_scale: float = 10.0          # acceleration scale of node inputs [m/s^2]
     norm: float = 32.0             # aggregation normaliser (sum / norm)
     scale: tuple = (1e-4, 1e-1, 1e-4, 1e-1)  # output scales: x fluid, v fluid, x DEM, v DEM
-    tol: float = 0.01              # judge: max |rho_new - rho_old| / rho0
+    tol: float = 0.01              # judge tolerance (fraction of rho0)
+    judge: int = 1                 # 1: max |rho - rho0| / rho0; 0: max change of rho over the jump
     edges_per_receiver: int = 160  # initial edge capacity per receiver
 
 
@@ -99,7 +101,7 @@ class Network:
         c = self.cfg
         return {"theta": self.theta.cpu().numpy(), "radius": c.radius, "dt": c.dt, "rho0": c.rho0,
                 "substeps": c.substeps, "v_scale": c.v_scale, "a_scale": c.a_scale, "norm": c.norm,
-                "scale": np.array(c.scale), "tol": c.tol}
+                "scale": np.array(c.scale), "tol": c.tol, "judge": c.judge}
 
     def save(self, path) -> None:
         np.savez(path, **self.state())
@@ -110,7 +112,8 @@ class Network:
         cfg = SurrogateConfig(radius=float(z["radius"]), dt=float(z["dt"]), rho0=float(z["rho0"]),
                               substeps=int(z["substeps"]), v_scale=float(z["v_scale"]),
                               a_scale=float(z["a_scale"]), norm=float(z["norm"]),
-                              scale=tuple(float(v) for v in z["scale"]), tol=float(z["tol"]))
+                              scale=tuple(float(v) for v in z["scale"]), tol=float(z["tol"]),
+                              judge=int(z["judge"]) if "judge" in z else 1)
         return Network(cfg, device, theta=z["theta"])
 
 
@@ -230,6 +233,7 @@ class Graph:
         a.node_pos3, a.node_pos4, a.node_vel4 = _lib.fptr(b["node_pos3"]), _lib.fptr(b["node_pos4"]), _lib.fptr(
             b["node_vel4"])
         a.x = C.cast(b["x"].data_ptr(), _lib.c_u16_p)
+        self.nodes = a
         _lib.check(self.lib.sphdem_mpnn_nodes(C.byref(a), self.stream()), "mpnn_nodes")
 
     def build(self, check: bool = True) -> None:
@@ -504,71 +508,97 @@ def train(net: Network, ts: TrainingSet, members, iters: int, lr: float = 1e-3, 
 # rollout: plain step + learned jump + density judge
 # ---------------------------------------------------------------------------
 class LearnedRollout:
-    """Advance a case with jumps of K = m + 1 steps (one plain, m learned)."""
+    """Advance a case with jumps of K = m + 1 steps (one plain, m learned).
+
+    Each jump is one call of sphdem_jump (a CUDA graph: plain step, network,
+    prior + correction, density judge); the host reads the judge's result and,
+    above ``tol`` (or on a graph-capacity overflow), undoes the jump and runs
+    the m steps with the plain method."""
 
     def __init__(self, case, net: Network):
+        from .engine import context_for
+
         self.case = case
         self.net = net
         self.cfg = net.cfg
-        self.g = Graph(net.cfg, net.device)
         self.lib = net.lib
+        self.g = Graph(net.cfg, net.device)
+        c = case
+        self.ctx = context_for(c.P, c.B, c.D, c.W, tuple(c.grids))
+        self.keep = torch.zeros(6 * c.P.n + 6 * c.D.n + c.P.n, dtype=torch.float32, device=net.device)
         self.dev = torch.zeros(1, dtype=torch.float32, device=net.device)
-        self.host = torch.zeros(2, dtype=torch.float32).pin_memory()
-        self.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0)
+        self.host = torch.zeros(3, dtype=torch.float32).pin_memory()
+        self.jump = None
+        self.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0)
 
-    def _density(self) -> None:
-        from .kernels import Kernel_density_sph
-
-        c = self.case
-        Kernel_density_sph(c.P, c.B, c.grids[0], c.grids[1], c.solv.support, c.solv.h)
+    def _setup(self) -> None:
+        c, g = self.case, self.g
+        self.ctx.set_params(c.solv, c.scales)
+        self.ctx.prepare(rebuild_moving=False,
+                         wall_key=(float(np.float32(c.solv.support)), float(np.float32(c.solv.h))))
+        g.set_nodes(Sets(c.P, c.B, c.D, c.W))
+        g.build(check=True)  # node grid geometry and edge capacity
+        j = _lib.JumpT()
+        j.nodes = g.nodes
+        j.net = g._net(self.net)
+        g.grid.fill(j.node_grid, g.n_nodes)
+        j.scan_scratch = _lib.iptr(g.scan)
+        j.graph_ctl = C.c_void_p(g.ctl.data_ptr())
+        j.radius = float(self.cfg.radius)
+        j.substeps = int(self.cfg.substeps)
+        for i in range(4):
+            j.scale[i] = float(self.cfg.scale[i])
+        j.keep = _lib.fptr(self.keep)
+        j.dev = _lib.fptr(self.dev)
+        j.judge = int(self.cfg.judge)
+        self.jump = j
 
     def run(self, first_step: int, n_steps: int) -> dict:
         c, cfg, lib = self.case, self.cfg, self.lib
-        P, D = c.P, c.D
-        m = cfg.substeps
+        m, K = cfg.substeps, cfg.substeps + 1
+        if self.jump is None:
+            self._setup()
+        ctx, D = self.ctx, c.D
         step, end = first_step, first_step + n_steps
-        sets = Sets(P, c.B, D, c.W)
-        inv = 1.0 / cfg.rho0
+        st = self.g.stream()
         while step < end:
-            c.run(step, 1)
-            step += 1
-            self.stats["plain_steps"] += 1
-            if end - step < m:
-                if end > step:
-                    c.run(step, end - step)
-                    self.stats["plain_steps"] += end - step
-                step = end
+            if end - step < K:
+                c.run(step, end - step)
+                self.stats["plain_steps"] += end - step
                 break
-            keep = (P.pos.clone(), P.vel.clone(), D.pos.clone(), D.vel.clone())
-            rho_old = P.rho.clone()
-            self.g.set_nodes(sets)
-            self.g.build(check=False)
-            out = self.g.forward(self.net)
-            _apply(lib, self.g, sets, out, cfg)
-            self._density()
-            self.dev.zero_()
-            _lib.check(lib.sphdem_mpnn_maxdev(_p(P.rho), _p(rho_old), P.n, inv, _p(self.dev), self.g.stream()),
-                       "mpnn_maxdev")
+            ctx.set_params(c.solv, c.scales)
+            _lib.check(lib.sphdem_jump(C.byref(ctx.ctx), C.byref(ctx.params), C.byref(self.jump), step, st),
+                       "sphdem_jump")
+            D._flip("dem")  # the plain step of the jump swapped both contact CSRs
+            D._flip("bnd")
             self.host[0:1].copy_(self.dev, non_blocking=True)
-            self.host[1:2].copy_(self.g.ctl[3:4].float(), non_blocking=True)
-            torch.cuda.current_stream().synchronize()
+            self.host[1:2].copy_(self.g.ctl[3:4], non_blocking=True)
+            self.host[2:3].copy_(ctx.ctl[3:4], non_blocking=True)
+            torch.cuda.current_stream(self.net.device).synchronize()
             self.stats["jumps"] += 1
-            if int(self.host[1].item()) & 0x8:  # graph capacity: undo, grow, plain steps
+            self.stats["plain_steps"] += 1
+            dev = float(self.host[0])
+            gflags, cflags = int(self.host[1]), int(self.host[2])
+            if cflags:
+                ctx._raise_for(cflags)
+            if gflags & 0x8:  # edge capacity: grow, re-capture, run this jump's substeps plain
                 self.g.ctl[3] = 0
                 self.g._alloc_edges(int(self.g.capacity * 1.5))
-                ok = False
-            else:
-                ok = float(self.host[0]) <= cfg.tol
-            if ok:
+                self.jump = None
+            elif gflags:
+                raise RuntimeError(f"learned jump raised device status 0x{gflags:x}")
+            if self.jump is not None and dev <= cfg.tol:
                 self.stats["learned_steps"] += m
+                self.stats["max_dev_accepted"] = max(self.stats["max_dev_accepted"], dev)
             else:
-                P.pos.copy_(keep[0])
-                P.vel.copy_(keep[1])
-                D.pos.copy_(keep[2])
-                D.vel.copy_(keep[3])
-                P.rho.copy_(rho_old)
+                _lib.check(lib.sphdem_jump_undo(C.byref(ctx.ctx), C.byref(self.jump or self._rebuild_jump()), st),
+                           "sphdem_jump_undo")
                 self.stats["fallbacks"] += 1
-                c.run(step, m)
+                c.run(step + 1, m)
                 self.stats["plain_steps"] += m
-            step += m
+            step += K
         return dict(self.stats)
+
+    def _rebuild_jump(self):
+        self._setup()
+        return self.jump
