@@ -458,10 +458,14 @@ def learned_arm(args, rank, world, local_rank):
     # the plain method's own density deviation at every jump boundary (untimed re-run)
     plain_final = plain.snapshot()
     plain.restore(snap0)
-    plain_dev = []
+    plain_dev, plain_change = [], []
+    rho_prev = None
     for s0 in range(0, n, K):
         plain.run(s0, min(K, n - s0))
         plain_dev.append((plain.P.rho - cfg.rho0).abs().max().item() / cfg.rho0)
+        if rho_prev is not None:
+            plain_change.append((plain.P.rho - rho_prev).abs().max().item() / cfg.rho0)
+        rho_prev = plain.P.rho.clone()
     plain.restore(plain_final)
     # learned: one plain step + m learned substeps per jump, density judge, plain fallback
     learned = Case(config_small(), device=device)
@@ -540,6 +544,9 @@ def learned_arm(args, rank, world, local_rank):
                            "judge_max_dev_accepted": stats["max_dev_accepted"]},
         "plain_density_deviation": {"max": max(plain_dev), "mean": sum(plain_dev) / len(plain_dev),
                                     "fraction_above_tol": sum(d > cfg.tol for d in plain_dev) / len(plain_dev)},
+        "plain_density_change_per_jump": {"max": max(plain_change), "mean": sum(plain_change) / len(plain_change),
+                                          "fraction_above_tol": sum(d > cfg.tol for d in plain_change)
+                                          / len(plain_change)},
         "rollout": stats,
         "training": {"members": len(members), "train_members": len(train_ids), "val_members": len(val_ids),
                      "trajectory_steps": args.train_steps, "iterations": args.train_iters,
@@ -656,8 +663,8 @@ def main():
     ap.add_argument("--train-iters", type=int, default=3000, help="learned: Adam iterations")
     ap.add_argument("--rollout-steps", type=int, default=1000, help="learned: steps of the compared rollouts")
     ap.add_argument("--judge-tol", type=float, default=0.01, help="learned: density judge tolerance / rho0")
-    ap.add_argument("--judge", type=int, default=1, choices=(0, 1),
-                    help="learned: 1 = density deviation |rho - rho0| / rho0, 0 = change over the jump")
+    ap.add_argument("--judge", type=int, default=0, choices=(0, 1),
+                    help="learned: 0 = density change over the jump, 1 = density deviation |rho - rho0| / rho0")
     ap.add_argument("--graph-radius", type=float, default=0.0, help="learned: edge radius (0 = SPH support)")
     ap.add_argument("--autotune", action="store_true",
                     help="time the launch candidates first (cached per case and GPU) and run the fastest")

@@ -80,7 +80,8 @@ def edge_features(pos4, vel4, send, recv, inv_r, inv_vs):
 def forward(theta, x, pos4, vel4, send, recv, n_recv, inv_r, inv_vs, inv_norm, quantize=False):
     """Network output [n_recv,16] and the activations the backward pass needs."""
     q = bf16 if quantize else _ident
-    W = {k: (q(v) if k in ("E1", "E2", "N1", "N2", "N3") else v) for k, v in unpack(theta).items()}
+    # the layer-1 edge bias rides in the tensor-core product (as a BF16 weight)
+    W = {k: (q(v) if k in ("E1", "E2", "N1", "N2", "N3", "b_E1") else v) for k, v in unpack(theta).items()}
     x = q(x)
     n = len(x)
     e = q(edge_features(pos4, vel4, send, recv, inv_r, inv_vs))

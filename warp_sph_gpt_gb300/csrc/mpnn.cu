@@ -51,6 +51,9 @@ constexpr int P_E1 = 0, P_E2 = 2048, P_E2T = 18432, P_N1 = 34816, P_N2 = 36864, 
 static_assert(P_N3T + 2048 == SPHDEM_MPNN_PACKED, "packed layout");
 
 enum { EPI_F32 = 0, EPI_SILU = 1 };
+// Edge-input column 7 is the constant 1 and the layer-1 image holds the bias
+// there, so the first edge MMA adds the bias itself.
+constexpr int kBiasCol = 7;
 enum { MODE_AGG = 0, MODE_SCATTER = 1 };
 
 // SiLU z * sigmoid(z) with the fast exponential and reciprocal (relative
@@ -142,7 +145,8 @@ __global__ void k_pack(const float* __restrict__ theta, uint16_t* __restrict__ p
     const int idx = blockIdx.x * blockDim.x + threadIdx.x;
     if (idx >= im.R * im.K) return;
     const int r = idx / im.K, k = idx % im.K;
-    const float w = im.trans ? theta[im.src + k * im.R + r] : theta[im.src + r * im.K + k];
+    float w = im.trans ? theta[im.src + k * im.R + r] : theta[im.src + r * im.K + k];
+    if (im.dst == P_E1 && k == kBiasCol) w = theta[SPHDEM_MPNN_E1_B + r];  // layer-1 bias rides in the MMA
     packed[im.dst + tile_off(r, k, im.K) / 2] = bf16_bits(w);
 }
 
@@ -290,49 +294,21 @@ __device__ __forceinline__ void edge_features(const EdgeArgs& a, int e, int E, i
     q0.x = pack2(dx * a.inv_r, dy * a.inv_r);
     q0.y = pack2(dz * a.inv_r, dist * a.inv_r);
     q0.z = pack2((vj.x - vr.x) * a.inv_vs, (vj.y - vr.y) * a.inv_vs);
-    q0.w = pack2((vj.z - vr.z) * a.inv_vs, 0.0f);
+    q0.w = pack2((vj.z - vr.z) * a.inv_vs, 1.0f);
 }
 
 constexpr uint32_t kImg16 = 128 * 16 * 2;   // 4 KB
 constexpr uint32_t kImg128 = 128 * 128 * 2;  // 32 KB
 // k_edges shared memory: the weight images once, then per pipeline an edge
 // feature tile, the hidden-activation tile, receiver/sender ids and an mbarrier.
+// The forward pass also stages the senders' latent rows (128 x 256 B) by
+// bulk copies issued when the tile is loaded, so they land during the MMAs.
 constexpr uint32_t EF_IMG1 = 0, EF_IMG2 = EF_IMG1 + kImg16, EF_B1 = EF_IMG2 + kImg128, EF_B2 = EF_B1 + 512,
-                   EF_BARS = EF_B2 + 512, EF_SLOT = EF_BARS + 32, EF_PIPE = (EF_SLOT + 16 + 1023) / 1024 * 1024,
+                   EF_BARS = EF_B2 + 512, EF_SLOT = EF_BARS + 48, EF_PIPE = (EF_SLOT + 16 + 1023) / 1024 * 1024,
                    EF_P_XS = 0, EF_P_ZR = EF_P_XS + kImg16, EF_P_SR = EF_P_ZR + kImg128, EF_P_SJ = EF_P_SR + 512,
-                   EF_P_BYTES = EF_P_SJ + 512, EF_BYTES = EF_PIPE + 2 * EF_P_BYTES;
-static_assert(EF_PIPE % 1024 == 0 && EF_P_BYTES % 16 == 0, "k_edges shared memory alignment");
-static_assert(2 * EF_BYTES <= 227 * 1024, "two k_edges CTAs per SM");
-
-// Barrier of one 128-thread pipeline (named barrier 1 or 2, immediate ids).
-__device__ __forceinline__ void pipe_sync(int id) {
-    if (id == 1)
-        asm volatile("bar.sync 1, 128;" ::: "memory");
-    else
-        asm volatile("bar.sync 2, 128;" ::: "memory");
-}
-__device__ __forceinline__ bool pipe_or(bool v, int id) {
-    uint32_t r;
-    if (id == 1)
-        asm volatile(
-            "{\n\t.reg .pred p, q;\n\t"
-            "setp.ne.u32 p, %1, 0;\n\t"
-            "bar.red.or.pred q, 1, 128, p;\n\t"
-            "selp.u32 %0, 1, 0, q;\n\t}"
-            : "=r"(r)
-            : "r"((uint32_t)v)
-            : "memory");
-    else
-        asm volatile(
-            "{\n\t.reg .pred p, q;\n\t"
-            "setp.ne.u32 p, %1, 0;\n\t"
-            "bar.red.or.pred q, 2, 128, p;\n\t"
-            "selp.u32 %0, 1, 0, q;\n\t}"
-            : "=r"(r)
-            : "r"((uint32_t)v)
-            : "memory");
-    return r != 0;
-}
+                   EF_P_H = EF_P_SJ + 512, EF_P_BYTES = EF_P_H + kImg128, EF_BYTES = EF_PIPE + 2 * EF_P_BYTES;
+static_assert(EF_PIPE % 1024 == 0 && EF_P_BYTES % 16 == 0 && EF_P_H % 16 == 0, "k_edges shared memory alignment");
+static_assert(EF_BYTES <= 227 * 1024, "k_edges shared memory");
 
 struct EdgeLoad {
     int r, j;
@@ -365,41 +341,77 @@ __device__ __forceinline__ uint4 edge_pack(const EdgeArgs& a, const EdgeLoad& L)
     const float dist = sqrtf(dx * dx + dy * dy + dz * dz);
     return make_uint4(pack2(dx * a.inv_r, dy * a.inv_r), pack2(dz * a.inv_r, dist * a.inv_r),
                       pack2((L.vj.x - L.vr.x) * a.inv_vs, (L.vj.y - L.vr.y) * a.inv_vs),
-                      pack2((L.vj.z - L.vr.z) * a.inv_vs, 0.0f));
+                      pack2((L.vj.z - L.vr.z) * a.inv_vs, 1.0f));
 }
 
-// Two independent pipelines of 4 warps per CTA (warps 0-3, 4-7), each owning
+// Two independent pipelines of 8 warps per CTA (warps 0-7, 8-15), each owning
 // TMEM columns [128 p, 128 p + 128): layer 1 lands there (lane = edge), is
-// consumed by its epilogue, and layer 2 (lane = feature) overwrites it.  The
-// next tile's edge data are loaded while the current tile's epilogue runs.
+// consumed by its epilogue, and layer 2 (lane = feature) overwrites it.  In
+// both epilogues warps w and w + 4 of a pipeline read the same 32 TMEM lanes
+// and split the 128 columns.  The next tile's edge data are loaded while the
+// current tile's epilogue runs; the senders' latent rows are bulk-copied into
+// shared memory as soon as a tile's edges are known.
+constexpr int kPT = 256;  // threads per pipeline
+
+// Barrier of one 256-thread pipeline (named barrier 1 or 2, immediate ids).
+__device__ __forceinline__ void pipe_sync256(int id) {
+    if (id == 1)
+        asm volatile("bar.sync 1, 256;" ::: "memory");
+    else
+        asm volatile("bar.sync 2, 256;" ::: "memory");
+}
+__device__ __forceinline__ bool pipe_or256(bool v, int id) {
+    uint32_t r;
+    if (id == 1)
+        asm volatile(
+            "{\n\t.reg .pred p, q;\n\t"
+            "setp.ne.u32 p, %1, 0;\n\t"
+            "bar.red.or.pred q, 1, 256, p;\n\t"
+            "selp.u32 %0, 1, 0, q;\n\t}"
+            : "=r"(r)
+            : "r"((uint32_t)v)
+            : "memory");
+    else
+        asm volatile(
+            "{\n\t.reg .pred p, q;\n\t"
+            "setp.ne.u32 p, %1, 0;\n\t"
+            "bar.red.or.pred q, 2, 256, p;\n\t"
+            "selp.u32 %0, 1, 0, q;\n\t}"
+            : "=r"(r)
+            : "r"((uint32_t)v)
+            : "memory");
+    return r != 0;
+}
+
 template <int MODE>
-__global__ void __launch_bounds__(2 * kT, 2) k_edges(EdgeArgs a) {
+__global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* img1 = sm + EF_IMG1;
     uint8_t* img2 = sm + EF_IMG2;
-    float* b1 = reinterpret_cast<float*>(sm + EF_B1);
     float* b2 = reinterpret_cast<float*>(sm + EF_B2);
-    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + EF_BARS);  // [0],[1] pipelines, [2] bulk copy
+    uint64_t* bars = reinterpret_cast<uint64_t*>(sm + EF_BARS);  // [0],[1] MMAs, [2] weights, [3],[4] sender rows
     uint32_t* slot = reinterpret_cast<uint32_t*>(sm + EF_SLOT);
-    const int tid = threadIdx.x, warp = tid >> 5, p = warp >> 2, lt = tid & (kT - 1);
+    const int tid = threadIdx.x, warp = tid >> 5, p = warp >> 3, plt = tid & (kPT - 1);
+    const int wq = warp & 7, lanes = 32 * (wq & 3), half = wq >> 2;
+    const int lt = plt & (kT - 1);  // TMEM lane of this thread
+    const bool loader = plt < kT;
     uint8_t* pb = sm + EF_PIPE + p * EF_P_BYTES;
     uint8_t* xs = pb + EF_P_XS;
     uint8_t* zr = pb + EF_P_ZR;
     int* sr = reinterpret_cast<int*>(pb + EF_P_SR);
     int* sj = reinterpret_cast<int*>(pb + EF_P_SJ);
+    uint8_t* hs = pb + EF_P_H;  // [128 edges][128] BF16 sender rows
     uint64_t* bar = &bars[p];
+    uint64_t* hbar = &bars[3 + p];
     const int bid = 1 + p;
     const int E = min(__ldg(a.offset + a.n_recv), a.cap);
 
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
-        mbar_init(&bars[2], 1);
+        for (int b = 0; b < 5; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
     }
     if (warp == 0) umma::tmem_alloc(slot, 256);
-    if (tid < 128) b1[tid] = a.b1[tid];
-    else b2[tid - 128] = a.b2[tid - 128];
+    if (tid < 128) b2[tid] = a.b2[tid];
     umma::fence_before();
     __syncthreads();
     umma::fence_after();
@@ -410,109 +422,116 @@ __global__ void __launch_bounds__(2 * kT, 2) k_edges(EdgeArgs a) {
         tma_load_1d(img2, a.img_e2, kImg128, &bars[2]);
     }
     bool failed = __syncthreads_or(!mbar_wait(&bars[2], 0, kPolls));
-    bool mine = true, pending = false;
-    uint32_t phase = 0;
+    bool mine = true, pending = false, hpending = false;
+    uint32_t phase = 0, hphase = 0;
     constexpr uint32_t idesc = umma::idesc_bf16(128, 128);
     const int stride = 2 * gridDim.x;
     int tile = 2 * blockIdx.x + p;
     EdgeLoad nxt;
-    edge_load_ids(a, tile * kT + lt, E, nxt);
-    edge_load_state(a, nxt);
+    nxt.r = nxt.j = -1;
+    if (loader) {
+        edge_load_ids(a, tile * kT + lt, E, nxt);
+        edge_load_state(a, nxt);
+    }
     for (; !failed && tile * kT < E; tile += stride) {
-        const EdgeLoad cur_e = nxt;
-        sr[lt] = cur_e.r;
-        sj[lt] = cur_e.j;
-        *reinterpret_cast<uint4*>(xs + tile_off(lt, 0, 16)) = edge_pack(a, cur_e);
-        *reinterpret_cast<uint4*>(xs + tile_off(lt, 8, 16)) = make_uint4(0, 0, 0, 0);
+        if (loader) {
+            const EdgeLoad cur_e = nxt;
+            sr[lt] = cur_e.r;
+            sj[lt] = cur_e.j;
+            *reinterpret_cast<uint4*>(xs + tile_off(lt, 0, 16)) = edge_pack(a, cur_e);
+            *reinterpret_cast<uint4*>(xs + tile_off(lt, 8, 16)) = make_uint4(0, 0, 0, 0);
+            if (MODE == MODE_AGG && lt == 0) {
+                const int valid = min(kT, E - tile * kT);
+                mbar_arrive_expect_tx(hbar, (uint32_t)valid * 256u);
+            }
+        }
         fence_proxy_async_smem();
         umma::fence_before();
-        pipe_sync(bid);
-        if (lt == 0) {
+        pipe_sync256(bid);
+        if (plt == 0) {
             umma::fence_after();
-            umma::mma_tile(tmem, xs, img1, 16, idesc, false);  // D[e][k]
+            umma::mma_tile(tmem, xs, img1, 16, idesc, false);  // D[e][k], layer-1 bias included
             umma::commit(bar);
         }
-        edge_load_ids(a, (tile + stride) * kT + lt, E, nxt);  // prefetch the next tile's ids
+        if (loader) {
+            if (MODE == MODE_AGG && sj[lt] >= 0) tma_load_1d(hs + lt * 256, a.h + (size_t)sj[lt] * kH, 256, hbar);
+            edge_load_ids(a, (tile + stride) * kT + lt, E, nxt);  // prefetch the next tile's ids
+        }
+        if (MODE == MODE_AGG) hpending = true;
         pending = true;
         mine = mbar_wait(bar, phase, kPolls);
-        if (pipe_or(!mine, bid)) { failed = true; break; }
+        if (pipe_or256(!mine, bid)) { failed = true; break; }
         phase ^= 1u;
         pending = false;
         umma::fence_after();
+        // layer-1 epilogue: lane = edge, this half's 64 hidden units
 #pragma unroll
-        for (int c0 = 0; c0 < 128; c0 += 32) {
+        for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
             float v[32];
-            umma::tmem_ld32(umma::taddr(tmem, 32 * (warp & 3), c0), v);
+            umma::tmem_ld32(umma::taddr(tmem, lanes, c0), v);
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const int k = c0 + 8 * q;
                 uint4 w;
-                w.x = pack2(fmaxf(v[8 * q] + b1[k], 0.f), fmaxf(v[8 * q + 1] + b1[k + 1], 0.f));
-                w.y = pack2(fmaxf(v[8 * q + 2] + b1[k + 2], 0.f), fmaxf(v[8 * q + 3] + b1[k + 3], 0.f));
-                w.z = pack2(fmaxf(v[8 * q + 4] + b1[k + 4], 0.f), fmaxf(v[8 * q + 5] + b1[k + 5], 0.f));
-                w.w = pack2(fmaxf(v[8 * q + 6] + b1[k + 6], 0.f), fmaxf(v[8 * q + 7] + b1[k + 7], 0.f));
+                w.x = pack2(fmaxf(v[8 * q], 0.f), fmaxf(v[8 * q + 1], 0.f));
+                w.y = pack2(fmaxf(v[8 * q + 2], 0.f), fmaxf(v[8 * q + 3], 0.f));
+                w.z = pack2(fmaxf(v[8 * q + 4], 0.f), fmaxf(v[8 * q + 5], 0.f));
+                w.w = pack2(fmaxf(v[8 * q + 6], 0.f), fmaxf(v[8 * q + 7], 0.f));
                 *reinterpret_cast<uint4*>(zr + tile_off(lt, k, 128)) = w;
             }
         }
         fence_proxy_async_smem();
         umma::fence_before();
-        pipe_sync(bid);
-        if (lt == 0) {
+        pipe_sync256(bid);
+        if (plt == 0) {
             umma::fence_after();
             umma::mma_tile(tmem, img2, zr, 128, idesc, false);  // D[c][e], over layer 1's columns
             umma::commit(bar);
         }
-        edge_load_state(a, nxt);  // and its particle state
+        if (loader) edge_load_state(a, nxt);  // the next tile's particle state
         pending = true;
         mine = mbar_wait(bar, phase, kPolls);
-        if (pipe_or(!mine, bid)) { failed = true; break; }
+        if (pipe_or256(!mine, bid)) { failed = true; break; }
         phase ^= 1u;
         pending = false;
         umma::fence_after();
-        // layer-2 epilogue: lane = feature c, columns = the tile's edges
+        // layer-2 epilogue: lane = feature c, this half's 64 edges of the tile
         const int c = lt;
         const float bc = b2[c];
         int cur = -1;
         float acc = 0.0f, gval = 0.0f;
         if (MODE == MODE_AGG) {
-            // gathers of the next 32 edges are in flight while these 32 are summed
-            uint16_t hn[32];
-#pragma unroll
-            for (int i = 0; i < 32; ++i) {
-                const int jj = sj[i];
-                hn[i] = jj >= 0 ? __ldg(a.h + (size_t)jj * kH + c) : (uint16_t)0;
-            }
-#pragma unroll
-            for (int c0 = 0; c0 < 128; c0 += 32) {
-                uint16_t hv[32];
-#pragma unroll
-                for (int i = 0; i < 32; ++i) hv[i] = hn[i];
-                if (c0 + 32 < 128) {
-#pragma unroll
-                    for (int i = 0; i < 32; ++i) {
-                        const int jj = sj[c0 + 32 + i];
-                        hn[i] = jj >= 0 ? __ldg(a.h + (size_t)jj * kH + c) : (uint16_t)0;
-                    }
-                }
+            const bool hmine = mbar_wait(hbar, hphase, kPolls);
+            if (pipe_or256(!hmine, bid)) { failed = true; break; }
+            hphase ^= 1u;
+            hpending = false;
+            const uint16_t* h16 = reinterpret_cast<const uint16_t*>(hs) + c;
+#pragma unroll 1
+            for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
                 float v[32];
-                umma::tmem_ld32(umma::taddr(tmem, 32 * (warp & 3), c0), v);
+                umma::tmem_ld32(umma::taddr(tmem, lanes, c0), v);
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const int rr = sr[c0 + i];
-                    if (rr < 0) continue;
-                    if (rr != cur) {
-                        if (cur >= 0) atomicAdd(a.agg + (size_t)cur * kH + c, acc * a.inv_norm);
-                        cur = rr;
-                        acc = 0.0f;
+                for (int i4 = 0; i4 < 32; i4 += 4) {
+                    const int4 r4 = *reinterpret_cast<const int4*>(sr + c0 + i4);
+                    const int rq[4] = {r4.x, r4.y, r4.z, r4.w};
+#pragma unroll
+                    for (int u = 0; u < 4; ++u) {
+                        const int i = i4 + u, rr = rq[u];
+                        if (rr < 0) continue;
+                        if (rr != cur) {
+                            if (cur >= 0) atomicAdd(a.agg + (size_t)cur * kH + c, acc * a.inv_norm);
+                            cur = rr;
+                            acc = 0.0f;
+                        }
+                        acc = fmaf(v[i] + bc, bf(h16[(c0 + i) * kH]), acc);
                     }
-                    acc = fmaf(v[i] + bc, bf(hv[i]), acc);
                 }
             }
         } else {
 #pragma unroll 1
-            for (int c0 = 0; c0 < 128; c0 += 32) {
+            for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
                 float v[32];
-                umma::tmem_ld32(umma::taddr(tmem, 32 * (warp & 3), c0), v);
+                umma::tmem_ld32(umma::taddr(tmem, lanes, c0), v);
 #pragma unroll 4
                 for (int i = 0; i < 32; ++i) {
                     const int rr = sr[c0 + i];
@@ -527,10 +546,11 @@ __global__ void __launch_bounds__(2 * kT, 2) k_edges(EdgeArgs a) {
         }
         if (MODE == MODE_AGG && cur >= 0) atomicAdd(a.agg + (size_t)cur * kH + c, acc * a.inv_norm);
         umma::fence_before();
-        pipe_sync(bid);
+        pipe_sync256(bid);
     }
-    if (failed && lt == 0) raise_flag(a.status, SPHDEM_FLAG_TIMEOUT);
+    if (failed && plt == 0) raise_flag(a.status, SPHDEM_FLAG_TIMEOUT);
     if (pending && !mine) mbar_wait(bar, phase, kPolls);
+    if (MODE == MODE_AGG && hpending) mbar_wait(hbar, hphase, kPolls);  // copies still landing
     umma::fence_before();
     __syncthreads();
     if (warp == 0) {
@@ -598,7 +618,7 @@ __global__ void __launch_bounds__(kT, 1) k_edges_bwd(EdgeArgs a) {
             const uint32_t w[4] = {q0.x, q0.y, q0.z, q0.w};
 #pragma unroll
             for (int i = 0; i < 16; ++i) {
-                const uint16_t hv = i < 8 ? (uint16_t)(w[i >> 1] >> (16 * (i & 1))) : (uint16_t)0;
+                const uint16_t hv = i < kBiasCol ? (uint16_t)(w[i >> 1] >> (16 * (i & 1))) : (uint16_t)0;
                 *reinterpret_cast<uint16_t*>(xt + tile_off(i, tid, 128)) = hv;
             }
         }
@@ -617,7 +637,7 @@ __global__ void __launch_bounds__(kT, 1) k_edges_bwd(EdgeArgs a) {
             float v[32];
             umma::tmem_ld32(umma::taddr(tmem, 32 * warp, c0), v);
 #pragma unroll
-            for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i] + b1[c0 + i], 0.0f);
+            for (int i = 0; i < 32; ++i) v[i] = fmaxf(v[i], 0.0f);
 #pragma unroll
             for (int q = 0; q < 4; ++q)
                 *reinterpret_cast<uint4*>(zr + tile_off(tid, c0 + 8 * q, 128)) =
@@ -1165,7 +1185,7 @@ template <int MODE>
 int edges(const EdgeArgs& a, int grid, cudaStream_t st) {
     int rc = smem_opt_in(k_edges<MODE>, EF_BYTES);
     if (rc) return rc;
-    k_edges<MODE><<<grid, 2 * kT, EF_BYTES, st>>>(a);
+    k_edges<MODE><<<grid, 2 * kPT, EF_BYTES, st>>>(a);
     return launch_status("mpnn edges");
 }
 
@@ -1245,7 +1265,7 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
                                            store_pre ? n->z0 : nullptr, n->status, st);
     if (rc) return rc;
     EdgeArgs a = edge_args(n);
-    const int eg = edge_grid(n, 2);
+    const int eg = edge_grid(n, 1);
     for (int round = 0; round < 2; ++round) {
         cudaError_t e = cudaMemsetAsync(n->agg, 0, sizeof(float) * (size_t)nr * kH, st);
         if (e != cudaSuccess) {
@@ -1295,7 +1315,7 @@ extern "C" int sphdem_mpnn_backward(const sphdem_mpnn_net_t* n, const sphdem_mpn
     EdgeArgs a = edge_args(n);
     a.g = g->g2;
     a.dh = g->d_h2;
-    if (nr > 0 && (rc = edges<MODE_SCATTER>(a, edge_grid(n, 2), st))) return rc;
+    if (nr > 0 && (rc = edges<MODE_SCATTER>(a, edge_grid(n, 1), st))) return rc;
     // second node layer
     k_act_grad<<<blocks_for(nh, 256), 256, 0, st>>>(g->d_h2, n->z2, nh, g->bf_a);
     if ((rc = wgrad<128>(g->bf_a, n->h1, nn, g->partial, ncta, n->status, st))) return rc;

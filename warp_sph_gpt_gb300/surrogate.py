@@ -11,9 +11,9 @@ current one.  One *jump* of K = m + 1 steps is
        x += m dt v + dt^2 a_s m(m+1)/2,  v += m dt a_s
      (the prior is what m symplectic-Euler substeps give if a_s stays fixed);
   3. the judge: the plain density kernel evaluated at the new positions.  If
-     the density deviation max_i |rho_i - rho0| / rho0 exceeds ``tol`` (or,
-     with judge = 0, any density moved by more than tol * rho0 over the
-     jump), the jump is undone and m plain steps run instead.
+     any fluid density moved by more than ``tol * rho0`` over the jump (or,
+     with judge = 1, if the density deviation max_i |rho_i - rho0| / rho0
+     exceeds tol), the jump is undone and m plain steps run instead.
 
 The plain step is therefore both the fallback and the judge of the density
 error.  The network is trained on trajectories of the batched plain solver
@@ -54,7 +54,7 @@ class SurrogateConfig:
     norm: float = 32.0             # aggregation normaliser (sum / norm)
     scale: tuple = (1e-4, 1e-1, 1e-4, 1e-1)  # output scales: x fluid, v fluid, x DEM, v DEM
     tol: float = 0.01              # judge tolerance (fraction of rho0)
-    judge: int = 1                 # 1: max |rho - rho0| / rho0; 0: max change of rho over the jump
+    judge: int = 0                 # 0: max change of rho over the jump; 1: max |rho - rho0| / rho0
     edges_per_receiver: int = 160  # initial edge capacity per receiver
 
 
@@ -113,7 +113,7 @@ class Network:
                               substeps=int(z["substeps"]), v_scale=float(z["v_scale"]),
                               a_scale=float(z["a_scale"]), norm=float(z["norm"]),
                               scale=tuple(float(v) for v in z["scale"]), tol=float(z["tol"]),
-                              judge=int(z["judge"]) if "judge" in z else 1)
+                              judge=int(z["judge"]) if "judge" in z else 0)
         return Network(cfg, device, theta=z["theta"])
 
 
