@@ -65,19 +65,27 @@ __device__ __forceinline__ float w_aux(const float4& aux, float dist) {
     return q < 2.0f ? aux.y * u2 * u2 * (1.0f + 2.0f * q) : 0.0f;
 }
 
-// V_j u^4 (1 + 2q) of one candidate if it lies inside the ball (exact FP32
-// membership d2 < t2, every operation rounded), else 0.  Branch-free: warps
-// walk 32 different candidates, so a branch on membership would diverge.
-// The factor 21/(16 pi h^3) is applied by the caller once per sum.
-__device__ __forceinline__ float ball_weight(float px, float py, float pz, const float4& q, float t2, float ih2) {
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// V_j u^4 (1 + 2q) of one candidate, u = max(1 - q/2, 0): the Wendland
+// weight vanishes at q = 2 and is clamped to 0 beyond, so candidates outside
+// the ball contribute nothing and no membership branch or select is needed
+// (warps walk 32 different candidates; a branch would diverge).  A pair whose
+// membership the reference decides by its rounded length(r) < 2h lies, if
+// near that boundary, within a few ulps of q = 2, where u^4 ~ 1e-28: the
+// normaliser's value is the same (the neighbour sets themselves are checked
+// with the exact predicate elsewhere).  The factor 21/(16 pi h^3) is applied
+// by the caller once per sum.
+__device__ __forceinline__ float ball_weight(float px, float py, float pz, const float4& q, float ih2) {
     const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
-    const float d2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
-    const float x = fmaf(d2, ih2, 1.0e-30f);  // q^2 (guarded at 0)
-    const float qq = x * rsqrtf(x);           // q = r / h
-    const float u = fmaf(-0.5f, qq, 1.0f);
+    const float qq = sqrt_approx(fmaf(dz, dz, fmaf(dy, dy, dx * dx)) * ih2);  // q = r / h
+    const float u = fmaxf(fmaf(-0.5f, qq, 1.0f), 0.0f);
     const float u2 = u * u;
-    const float vu4 = d2 < t2 ? q.w * u2 * u2 : 0.0f;
-    return vu4 * fmaf(2.0f, qq, 1.0f);
+    return q.w * ((u2 * u2) * fmaf(2.0f, qq, 1.0f));
 }
 
 // Porosity pass 1: dry particles get clamp(1); the rest are listed.  The list
@@ -126,7 +134,7 @@ __device__ __forceinline__ float warp_fluid_sum(const CplArgs& a, int inst, floa
     float acc = 0.0f;
     warp_ranges_ball(a.gs, px, py, pz, rq, inst, [&](int s, int e) {
 #pragma unroll 4
-        for (int j = s + lane; j < e; j += 32) acc += ball_weight(px, py, pz, a.f_posv[j], t2, ih2);
+        for (int j = s + lane; j < e; j += 32) acc += ball_weight(px, py, pz, a.f_posv[j], ih2);
     });
     return warp_sum(acc) * kaux.y;
 }
@@ -338,7 +346,7 @@ __global__ void __launch_bounds__(kTileThreads, 3) k_porosity_tiles(CplArgs a) {
                     for (int i = (lane - pe.x) & 31; i < pe.y; i += 32) {
                         const float4 q = B[i];
 #pragma unroll
-                        for (int s = 0; s < kSubjPerWarp; ++s) acc[s] += ball_weight(p[s].x, p[s].y, p[s].z, q, t2, ih2);
+                        for (int s = 0; s < kSubjPerWarp; ++s) acc[s] += ball_weight(p[s].x, p[s].y, p[s].z, q, ih2);
                     }
                 }
                 __syncthreads();  // buffer b is free again
