@@ -255,6 +255,8 @@ def gpu_arm(args, rank, world, local_rank):
     runner = make_runner(args.workload, device, args.cell_factor)
     if not tuning:
         tuning = {"lanes_sph": args.lanes_sph or default_lanes(runner.P.n)}
+        if args.porosity_variant >= 0:
+            tuning["porosity_variant"] = args.porosity_variant
     runner.tune(tuning)
     gen, solv, desc = runner.gen, runner.solv, runner.desc
     P, B, D, W = runner.P, runner.B, runner.D, runner.W
@@ -671,6 +673,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--porosity-variant", type=int, default=-1, choices=(-1, 0, 1),
+                    help="porosity normaliser implementation (-1 = library default)")
     ap.add_argument("--lanes-sph", type=int, default=0, choices=(0, 1, 32),
                     help="threads per particle of the SPH loops (0 = by system size)")
     ap.add_argument("--cell-factor", type=float, default=1.0,

@@ -139,7 +139,10 @@ __device__ __forceinline__ float warp_fluid_sum(const CplArgs& a, int inst, floa
     return warp_sum(acc) * kaux.y;
 }
 
-// Porosity pass 2: one warp per listed particle.
+// Porosity pass 2: one warp per listed particle.  UNIFORM: one DEM h for all
+// spheres (the normaliser is one sum per particle); otherwise each DEM in
+// reach has its own normaliser sum.
+template <bool UNIFORM>
 __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
     const int lane = threadIdx.x & 31;
     const int warps = gridDim.x * (blockDim.x >> 5);
@@ -151,7 +154,7 @@ __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
         const float4 p = a.f_posv[k];
         const int inst = inst_of(a.gs, o);
         float flt = 0.0f;
-        if (a.h > 0.0f) flt = warp_fluid_sum(a, inst, p.x, p.y, p.z, a.rq, a.t_support, kuni);
+        if (UNIFORM) flt = warp_fluid_sum(a, inst, p.x, p.y, p.z, a.rq, a.t_support, kuni);
         float solid = 0.0f;
         const Win w = window(a.gd, p.x, p.y, p.z, a.rq);
         for_each_range(a.gd, w, inst, [&](int s, int e) {
@@ -162,8 +165,7 @@ __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
                 const float4 ab = a.aux[b];
                 if (r.d2 < ab.z) {
                     float local_flt = flt;
-                    if (a.h <= 0.0f)
-                        local_flt = warp_fluid_sum(a, inst, p.x, p.y, p.z, pad_radius(ab.w), ab.z, ab);
+                    if (!UNIFORM) local_flt = warp_fluid_sum(a, inst, p.x, p.y, p.z, pad_radius(ab.w), ab.z, ab);
                     solid += a.D.volume[b] * w_aux(ab, fast_sqrt(r.d2)) / (local_flt + 1.0e-20f);
                 }
             }
@@ -550,7 +552,10 @@ int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, f
             const int need = blocks_for(n, 8);
             int blocks = sms * 8;
             if (need < blocks) blocks = need;
-            k_porosity_near<<<blocks, 256, 0, st>>>(a);
+            if (a.h > 0.0f)
+                k_porosity_near<true><<<blocks, 256, 0, st>>>(a);
+            else
+                k_porosity_near<false><<<blocks, 256, 0, st>>>(a);
         }
     }
     return launch_status("porosity");
