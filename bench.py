@@ -223,6 +223,44 @@ def reduce_max(value: float, world: int, device=None) -> float:
     return float(t.item())
 
 
+# FP32 operations per candidate of the porosity normaliser's inner loop
+# (csrc/coupling.cu ball_weight + accumulate: 3 sub, 1 mul + 2 fma for d2,
+# 1 mul by 1/h^2, 1 fma + 1 max for u, 2 mul for u^4, 1 fma for 1 + 2q, 1 mul,
+# 1 fma into the sum), plus one MUFU square root.
+POROSITY_FP32_OPS_PER_PAIR = 14
+
+
+def porosity_compute_roofline(ctx, D, scales, porosity_ms: float, device):
+    """The porosity normaliser is bound by FP32 issue, not HBM: pairs summed
+    per second against the FP32 lane rate / ops per pair.  Pairs are estimated
+    from an exact count over 256 sampled listed particles."""
+    import torch
+
+    if D.n == 0 or porosity_ms <= 0 or scales[3] <= 0:
+        return None
+    n_near = int(ctx.ctl[6].item())
+    if n_near <= 0:
+        return None
+    w = ctx.work
+    g = torch.Generator(device="cpu").manual_seed(0)
+    pick = torch.randperm(n_near, generator=g)[:256].to(device)
+    subj = w["f_posv"][w["near_list"][:n_near][pick].long(), :3]
+    fluid = w["f_posv"][:, :3]
+    support = 2.0 * float(scales[3])
+    counts = torch.cat([(torch.cdist(subj[i:i + 32], fluid) < support).sum(1) for i in range(0, len(subj), 32)])
+    pairs = float(counts.float().mean().item()) * n_near
+    props = torch.cuda.get_device_properties(device)
+    peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
+    mhz = float(peaks.get("sm_max_mhz", 2070.0))
+    lanes = props.multi_processor_count * 128
+    peak_pairs = lanes * mhz * 1e6 / POROSITY_FP32_OPS_PER_PAIR
+    achieved = pairs / (porosity_ms * 1e-3)
+    return {"bound": "fp32", "kernel": "k_porosity_near", "listed_particles": n_near,
+            "pairs_per_step": pairs, "achieved_pairs_per_s": achieved, "peak_pairs_per_s": peak_pairs,
+            "frac": achieved / peak_pairs, "fp32_ops_per_pair": POROSITY_FP32_OPS_PER_PAIR,
+            "peak_basis": f"{props.multi_processor_count} SMs x 128 FP32 lanes x {mhz:.0f} MHz"}
+
+
 def job_throughput(units_per_replica: int, steps: int, world: int, ms_max: float) -> float:
     """Whole-job particle-steps/s of `world` replicas timed by the slowest."""
     return world * units_per_replica * steps / (ms_max * 1e-3)
@@ -314,6 +352,8 @@ def gpu_arm(args, rank, world, local_rank):
     peak, peak_kind = peak_hbm()
     achieved = alg_bytes / (phases[dom] * 1e-3) / 1e9 if phases[dom] > 0 else 0.0
 
+    compute = porosity_compute_roofline(ctx, D, scales, phases.get("porosity", 0.0), device)
+
     # e2e through the public API with host buffers
     e2e_steps = min(args.steps, args.e2e_steps)
     host = {k: torch.empty_like(t, device="cpu").pin_memory() for k, t in
@@ -369,6 +409,7 @@ def gpu_arm(args, rank, world, local_rank):
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "traffic": profile_traffic(dom, args.workload)},
+        "compute_roofline": compute,
         "phases_ms": phases,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
