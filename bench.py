@@ -703,12 +703,13 @@ def main():
     ap.add_argument("--workload", default="large800k", choices=WORKLOADS)
     ap.add_argument("--train-members", type=int, default=64, help="learned: ensemble members of training data")
     ap.add_argument("--train-steps", type=int, default=1000, help="learned: plain steps per training trajectory")
-    ap.add_argument("--train-iters", type=int, default=3000, help="learned: Adam iterations")
+    ap.add_argument("--train-iters", type=int, default=10000, help="learned: Adam iterations")
     ap.add_argument("--rollout-steps", type=int, default=1000, help="learned: steps of the compared rollouts")
     ap.add_argument("--judge-tol", type=float, default=0.01, help="learned: density judge tolerance / rho0")
     ap.add_argument("--judge", type=int, default=0, choices=(0, 1),
                     help="learned: 0 = density change over the jump, 1 = density deviation |rho - rho0| / rho0")
-    ap.add_argument("--graph-radius", type=float, default=0.0, help="learned: edge radius (0 = SPH support)")
+    ap.add_argument("--graph-radius", type=float, default=0.04,
+                    help="learned: edge radius in m (0 = the SPH support 2h); 0.04 = 2 dx at config 1")
     ap.add_argument("--autotune", action="store_true",
                     help="time the launch candidates first (cached per case and GPU) and run the fastest")
     ap.add_argument("--e2e-steps", type=int, default=20)
