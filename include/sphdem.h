@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPHDEM_ABI_VERSION 6
+#define SPHDEM_ABI_VERSION 7
 
 /* ---- return codes ---------------------------------------------------- */
 #define SPHDEM_OK                0
@@ -195,6 +195,8 @@ typedef struct sphdem_work {
     /* DEM scratch, point order */
     int32_t* dem_count; /* [2*(n_dem+1)] per-row contact counts               */
     float* dem_aux;     /* [n_dem,4] 1/h, 21/(16 pi h^3), sqrt bound of 2h, 2h  */
+    /* fluid, in grid_sph order, uniform DEM h only */
+    float* f_posq;      /* [n_sph,4] x/h, y/h, z/h, m/rho (porosity sums)     */
 } sphdem_work_t;
 
 /* Solver controls.  Reference: Solv (input/Config.py:11-49 with the SPH-DEM

@@ -61,7 +61,7 @@ class WorkT(C.Structure):
     _fields_ = [("f_posm", c_float_p), ("f_vel", c_float_p), ("f_rp", c_float_p), ("f_vprev", c_float_p),
                 ("f_posv", c_float_p), ("f_pgf", c_float_p), ("near_list", c_int_p),
                 ("b_posm", c_float_p), ("b_vel", c_float_p), ("b_rp", c_float_p), ("b_vprev", c_float_p),
-                ("b_self", c_float_p), ("dem_count", c_int_p), ("dem_aux", c_float_p)]
+                ("b_self", c_float_p), ("dem_count", c_int_p), ("dem_aux", c_float_p), ("f_posq", c_float_p)]
 
 
 class ParamsT(C.Structure):
@@ -119,7 +119,7 @@ FLAG_CSR_DEM_OVERFLOW = 0x1
 FLAG_CSR_BND_OVERFLOW = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_TIMEOUT = 0x10
-ABI_VERSION = 6
+ABI_VERSION = 7
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
 REL = dict(SPH_SPH_SUPPORT=0, SPH_BND_SUPPORT=1, BND_SPH_SUPPORT=2, BND_BND_SUPPORT=3, SPH_SPH_FORCE=4,

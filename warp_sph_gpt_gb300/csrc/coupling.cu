@@ -47,6 +47,7 @@ struct CplArgs {
     const float4* __restrict__ f_posv;  // x, y, z, m/rho
     const float4* __restrict__ f_vel;
     const float4* __restrict__ f_pgf;   // pgf, rho
+    float4* f_posq;                     // x/h, y/h, z/h, m/rho (uniform h: written by k_near)
     const float4* __restrict__ aux;     // per DEM: 1/h, cw, sqrt bound of 2h, 2h
     sphdem_sph_t P;
     sphdem_dem_t D;
@@ -88,6 +89,15 @@ __device__ __forceinline__ float ball_weight(float px, float py, float pz, const
     return q.w * ((u2 * u2) * fmaf(2.0f, qq, 1.0f));
 }
 
+// The same for coordinates already in units of h (p and q scaled by 1/h).
+__device__ __forceinline__ float ball_weight_h(float px, float py, float pz, const float4& q) {
+    const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
+    const float qq = sqrt_approx(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
+    const float u = fmaxf(fmaf(-0.5f, qq, 1.0f), 0.0f);
+    const float u2 = u * u;
+    return q.w * ((u2 * u2) * fmaf(2.0f, qq, 1.0f));
+}
+
 // Porosity pass 1: dry particles get clamp(1); the rest are listed.  The list
 // keeps slot order inside each block of 256 slots (ordered block compaction),
 // so consecutive entries are neighbours in space.
@@ -100,6 +110,10 @@ __global__ void __launch_bounds__(256) k_near(CplArgs a) {
     if (k < a.P.n) {
         o = a.gs.order[k];
         const float4 p = a.f_posv[k];
+        if (a.h > 0.0f && a.f_posq) {  // positions in units of the uniform coupling h
+            const float ih = a.kern.inv_h;
+            a.f_posq[k] = make_float4(p.x * ih, p.y * ih, p.z * ih, p.w);
+        }
         const int inst = inst_of(a.gs, o);
         if (a.D.n > 0) {
             const Win w = window(a.gd, p.x, p.y, p.z, a.rq);
@@ -154,7 +168,17 @@ __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
         const float4 p = a.f_posv[k];
         const int inst = inst_of(a.gs, o);
         float flt = 0.0f;
-        if (UNIFORM) flt = warp_fluid_sum(a, inst, p.x, p.y, p.z, a.rq, a.t_support, kuni);
+        if (UNIFORM) {
+            // candidates from the scaled copy: the column walk uses world coordinates
+            const float ih = a.kern.inv_h;
+            const float sx = p.x * ih, sy = p.y * ih, sz = p.z * ih;
+            float acc = 0.0f;
+            warp_ranges_ball(a.gs, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
+#pragma unroll 4
+                for (int j = s + lane; j < e; j += 32) acc += ball_weight_h(sx, sy, sz, a.f_posq[j]);
+            });
+            flt = warp_sum(acc) * kuni.y;
+        }
         float solid = 0.0f;
         const Win w = window(a.gd, p.x, p.y, p.z, a.rq);
         for_each_range(a.gd, w, inst, [&](int s, int e) {
@@ -505,6 +529,7 @@ CplArgs make_args(const sphdem_ctx_t* c, float support, float h) {
     a.f_posv = (const float4*)c->work.f_posv;
     a.f_vel = (const float4*)c->work.f_vel;
     a.f_pgf = (const float4*)c->work.f_pgf;
+    a.f_posq = (float4*)c->work.f_posq;
     a.aux = (const float4*)c->work.dem_aux;
     a.P = c->sph;
     a.D = c->dem;

@@ -63,7 +63,8 @@ class StepContext:
             f_vprev=torch.zeros(ns, **f), f_posv=torch.zeros((ns, 4), **f), f_pgf=torch.zeros((ns, 4), **f),
             near_list=torch.zeros(ns, **i), b_posm=torch.zeros((nb, 4), **f), b_vel=torch.zeros((nb, 4), **f),
             b_rp=torch.zeros((nb, 4), **f), b_vprev=torch.zeros(nb, **f), b_self=torch.zeros(nb, **f),
-            dem_count=torch.zeros(2 * (nd + 1), **i), dem_aux=torch.zeros((nd, 4), **f))
+            dem_count=torch.zeros(2 * (nd + 1), **i), dem_aux=torch.zeros((nd, 4), **f),
+            f_posq=torch.zeros((ns, 4), **f))
 
     def _domain(self):
         """Union bounding box of all particle sets (one host sync, once)."""
