@@ -469,9 +469,26 @@ def learned_arm(args, rank, world, local_rank):
     net = S.Network(cfg, device, seed=0)
     prior = S.evaluate(net, ts, val_ids, zero=True)
     t0 = time.perf_counter()
-    hist = S.train(net, ts, train_ids, iters=args.train_iters, lr=2e-3, log=log, log_every=500)
+    hist = S.train(net, ts, train_ids, iters=args.train_iters, lr=2e-3, log=log, log_every=500,
+                   edge_weight=args.edge_weight, noise=(args.noise_x, args.noise_v))
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
+    on_policy = []
+    if args.dagger_rounds > 0:
+        cases = []
+        for i in [i for i in train_ids if len(members[i][1])][: args.dagger_cases]:  # members with DEM
+            gen_i, pos_i, rad_i = members[i]
+            c = Case(gen_i, pos_i, rad_i, device=device)
+            c.tune({"lanes_sph": default_lanes(c.P.n)})
+            cases.append(c)
+        for rnd in range(args.dagger_rounds):
+            snaps0 = [c.snapshot() for c in cases]
+            on_policy += S.collect_on_policy(net, cases, args.train_steps, log=log)
+            for c, s0 in zip(cases, snaps0):
+                c.restore(s0)
+            hist += S.train(net, ts, train_ids, iters=args.dagger_iters, lr=1e-3, log=log, log_every=1000,
+                            edge_weight=args.edge_weight, extra=on_policy, seed=rnd + 1)
+        t_train = time.perf_counter() - t0
     val = S.evaluate(net, ts, val_ids)
     log(f"held-out one-jump loss: prior {prior:.4f} -> trained {val:.4f}")
     del ts, ens
@@ -575,7 +592,8 @@ def learned_arm(args, rank, world, local_rank):
         "data": "synthetic (seeded generator rules; training trajectories from the batched plain solver)",
         "config": {"workload": "learned K-step surrogate vs plain on the config-1 dam break "
                                "(12,500 fluid, 20 DEM, dt=1e-4)", "K": K, "judge_tol": cfg.tol, "judge": cfg.judge,
-                   "graph_radius": cfg.radius,
+                   "graph_radius": cfg.radius, "edge_weight": args.edge_weight,
+                   "train_noise": [args.noise_x, args.noise_v], "dagger_rounds": args.dagger_rounds,
                    "rollout_steps": n, "fluid": learned.P.n, "dem": learned.D.n,
                    "l2": "state < L2 (resident between steps, as in a run)"},
         "plain": {"value": units * n / t_plain, "ms_per_step": t_plain * 1e3 / n, "clocks": clocks_plain.summary()},
@@ -594,7 +612,8 @@ def learned_arm(args, rank, world, local_rank):
         "training": {"members": len(members), "train_members": len(train_ids), "val_members": len(val_ids),
                      "trajectory_steps": args.train_steps, "iterations": args.train_iters,
                      "generate_s": round(t_gen, 2), "train_s": round(t_train, 2),
-                     "val_loss_prior": prior, "val_loss_trained": val, "loss_history": hist[-3:]},
+                     "val_loss_prior": prior, "val_loss_trained": val, "loss_history": hist[-3:],
+                     "output_scales": list(cfg.scale)},
         "roofline": {"bound": "tensor", "kernel_phase": "mpnn forward (k_rows, k_edges)", "achieved": achieved_tf,
                      "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
                      "peak_source": "measured" if peaks else "fallback", "flops_per_launch": flops,
@@ -706,6 +725,14 @@ def main():
     ap.add_argument("--train-iters", type=int, default=10000, help="learned: Adam iterations")
     ap.add_argument("--rollout-steps", type=int, default=1000, help="learned: steps of the compared rollouts")
     ap.add_argument("--judge-tol", type=float, default=0.01, help="learned: density judge tolerance / rho0")
+    ap.add_argument("--dagger-rounds", type=int, default=2,
+                    help="learned: rounds of on-policy data (states of judged learned rollouts + plain targets)")
+    ap.add_argument("--dagger-cases", type=int, default=16, help="learned: training members rolled out per round")
+    ap.add_argument("--dagger-iters", type=int, default=4000, help="learned: Adam iterations per on-policy round")
+    ap.add_argument("--noise-x", type=float, default=0.0, help="learned: training input noise on positions [m]")
+    ap.add_argument("--noise-v", type=float, default=0.0, help="learned: training input noise on velocities [m/s]")
+    ap.add_argument("--edge-weight", type=float, default=0.0,
+                    help="learned: weight of the neighbour relative-displacement term of the training loss")
     ap.add_argument("--judge", type=int, default=0, choices=(0, 1),
                     help="learned: 0 = density change over the jump, 1 = density deviation |rho - rho0| / rho0")
     ap.add_argument("--graph-radius", type=float, default=0.04,

@@ -137,6 +137,14 @@ int sphdem_mpnn_backward(const sphdem_mpnn_net_t* net, const sphdem_mpnn_grad_t*
 int sphdem_mpnn_loss(const float* out, const float* target, int32_t n, float* loss, float* d_out,
                      sphdem_stream_t stream);
 
+/* Adds lambda / E * sum over the graph's edges (i <- j) of |dx_i - dx_j|^2,
+ * dx = out[:, 0:3] - target[:, 0:3] (dx_j = 0 for senders that are not
+ * receivers), to *loss and its gradient to d_out: relative displacement
+ * errors between neighbours are what changes their SPH density. */
+int sphdem_mpnn_edge_loss(const int32_t* offset, const int32_t* sender, const int32_t* receiver, int32_t n_recv,
+                          int32_t edge_capacity, const float* out, const float* target, float lambda, float* loss,
+                          float* d_out, sphdem_stream_t stream);
+
 /* One Adam step (bias-corrected, step >= 1) on n parameters. */
 int sphdem_mpnn_adam(float* theta, const float* grad, float* m, float* v, int32_t n, float lr, float beta1,
                      float beta2, float eps, int32_t step, sphdem_stream_t stream);

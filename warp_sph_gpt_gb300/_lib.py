@@ -168,6 +168,8 @@ _SIGNATURES = {
     "sphdem_mpnn_forward": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
     "sphdem_mpnn_backward": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_mpnn_loss": ([C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_mpnn_edge_loss": ([C.c_void_p] * 3 + [C.c_int32, C.c_int32, C.c_void_p, C.c_void_p, C.c_float,
+                                                   C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_mpnn_adam": ([C.c_void_p] * 4 + [C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float, C.c_int32,
                                              C.c_void_p], C.c_int),
     "sphdem_mpnn_apply": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p,

@@ -917,6 +917,34 @@ __global__ void __launch_bounds__(1024) k_loss(const float* __restrict__ out, co
     }
 }
 
+// Edge term of the loss: lambda / E * sum over edges (i <- j) of
+// |dx_i - dx_j|^2, dx = out[:, 0:3] - target[:, 0:3] (senders that are not
+// receivers do not move: dx_j = 0).  Adds its gradient to d_out and its value
+// to *loss (atomics: the order of the FP32 additions is not fixed).
+__global__ void k_edge_loss(const int* __restrict__ offset, const int* __restrict__ sender,
+                            const int* __restrict__ receiver, int n_recv, int cap, const float* __restrict__ out,
+                            const float* __restrict__ target, float lambda, float* __restrict__ d_out,
+                            float* __restrict__ loss) {
+    const int E = min(offset[n_recv], cap);
+    const float w = E > 0 ? lambda / (float)E : 0.0f;
+    float part = 0.0f;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
+        const int i = receiver[e], j = sender[e];
+        const bool jr = j < n_recv;
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float di = out[16 * i + d] - target[16 * i + d];
+            const float dj = jr ? out[16 * j + d] - target[16 * j + d] : 0.0f;
+            const float g = di - dj;
+            part += g * g;
+            atomicAdd(d_out + 16 * i + d, 2.0f * w * g);
+            if (jr) atomicAdd(d_out + 16 * j + d, -2.0f * w * g);
+        }
+    }
+    part = warp_sum(part * w);
+    if ((threadIdx.x & 31) == 0 && part != 0.0f) atomicAdd(loss, part);
+}
+
 __global__ void k_adam(float* __restrict__ th, const float* __restrict__ g, float* __restrict__ m,
                        float* __restrict__ v, int n, float lr, float b1, float b2, float eps, float c1, float c2) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1372,6 +1400,21 @@ extern "C" int sphdem_mpnn_loss(const float* out, const float* target, int32_t n
     }
     k_loss<<<1, 1024, 0, as_stream(stream)>>>(out, target, n, loss, d_out);
     return launch_status("mpnn_loss");
+}
+
+extern "C" int sphdem_mpnn_edge_loss(const int32_t* offset, const int32_t* sender, const int32_t* receiver,
+                                     int32_t n_recv, int32_t edge_capacity, const float* out, const float* target,
+                                     float lambda, float* loss, float* d_out, sphdem_stream_t stream) {
+    if (!offset || !sender || !receiver || !out || !target || !loss || !d_out || n_recv < 0 || edge_capacity < 0) {
+        set_error_msg("mpnn_edge_loss: invalid arguments");
+        return SPHDEM_ERR_INVALID;
+    }
+    if (n_recv == 0 || edge_capacity == 0) return SPHDEM_OK;
+    int grid = blocks_for(edge_capacity, 256);
+    if (grid > 8 * sm_count()) grid = 8 * sm_count();
+    k_edge_loss<<<grid, 256, 0, as_stream(stream)>>>(offset, sender, receiver, n_recv, edge_capacity, out, target,
+                                                    lambda, d_out, loss);
+    return launch_status("mpnn_edge_loss");
 }
 
 extern "C" int sphdem_mpnn_adam(float* theta, const float* grad, float* m, float* v, int32_t n, float lr, float beta1,

@@ -320,6 +320,16 @@ class Graph:
                                              self.stream()), "mpnn_loss")
         return b["loss"]
 
+    def edge_loss(self, lam: float, target: torch.Tensor = None) -> torch.Tensor:
+        """Adds the edge term (relative displacement errors of neighbours) to the
+        loss and d_out of the last loss() call."""
+        b = self.buf
+        t = target if target is not None else b["target"]
+        _lib.check(self.lib.sphdem_mpnn_edge_loss(_p(b["offset"]), _p(b["sender"]), _p(b["receiver"]), self.n_recv,
+                                                  self.capacity, _p(b["out"]), _p(t), float(lam), _p(b["loss"]),
+                                                  _p(b["d_out"]), self.stream()), "mpnn_edge_loss")
+        return b["loss"]
+
     def status(self) -> int:
         return int(self.ctl[3].item())
 
@@ -425,6 +435,55 @@ def sample_sets(ts: TrainingSet, snap: Snapshot, k: int):
     return sets, snap.x_t[r0:r1], snap.v_t[r0:r1]
 
 
+def collect_on_policy(net: Network, cases, n_steps: int, log=None) -> list:
+    """Samples from the states a judged learned rollout visits (dataset
+    aggregation): along each case's rollout, the state after every plain step
+    is paired with the plain method's own continuation m steps later; the
+    rollout then moves on with the learned jump if the density judge accepts
+    it, else with that plain continuation.  Returns [(sets, x_t, v_t), ...]."""
+    from .kernels import Kernel_density_sph
+
+    cfg, lib = net.cfg, net.lib
+    m, K = cfg.substeps, cfg.substeps + 1
+    g = Graph(cfg, net.device)
+    out_samples = []
+    accepted = total = 0
+    t0 = time.perf_counter()
+    for case in cases:
+        P, B, D, W = case.P, case.B, case.D, case.W
+        step = 0
+        while step + K <= n_steps:
+            case.run(step, 1)
+            st = case.snapshot()
+            case.run(step + 1, m)
+            x_t = torch.cat([P.pos, D.pos]).clone()
+            v_t = torch.cat([P.vel, D.vel]).clone()
+            plain_next = case.snapshot()
+            sets = Sets(_Proxy(P, pos=st[("P", "pos")], vel=st[("P", "vel")], acc=st[("P", "acc")],
+                               rho=st[("P", "rho")], porosity=st[("P", "porosity")]),
+                        _Proxy(B, rho=st[("B", "rho")]),
+                        _Proxy(D, pos=st[("D", "pos")], vel=st[("D", "vel")], acc=st[("D", "acc")]), W)
+            out_samples.append((sets, x_t, v_t))
+            # the learned jump from the same state, judged like a rollout
+            case.restore(st)
+            live = Sets(P, B, D, W)
+            g.set_nodes(live)
+            g.build()
+            _apply(lib, g, live, g.forward(net), cfg)
+            Kernel_density_sph(P, B, case.grids[0], case.grids[1], case.solv.support, case.solv.h)
+            dev = ((P.rho - st[("P", "rho")]).abs().max() / cfg.rho0).item()
+            total += 1
+            if dev <= cfg.tol:
+                accepted += 1
+            else:
+                case.restore(plain_next)
+            step += K
+    if log:
+        log(f"on-policy: {len(out_samples)} samples from {len(cases)} cases, {accepted}/{total} jumps accepted, "
+            f"{time.perf_counter() - t0:.1f} s")
+    return out_samples
+
+
 def prepare_target(lib, g: Graph, sets: Sets, x_t, v_t, cfg: SurrogateConfig) -> None:
     _apply(lib, g, sets, None, cfg, target_state=(x_t, v_t))
 
@@ -475,23 +534,62 @@ def evaluate(net: Network, ts: TrainingSet, members, graph: Graph = None, zero: 
     return tot / max(cnt, 1)
 
 
+def _noisy(sets: Sets, sigma_x: float, sigma_v: float, gen) -> Sets:
+    """The sample with Gaussian noise on fluid and DEM positions and
+    velocities (the target stays the true future state, so the network learns
+    to correct perturbed inputs -- as a rollout feeds it its own errors)."""
+    def jitter(t, s):
+        return t + s * torch.randn(t.shape, device=t.device, generator=gen) if s > 0 else t
+    a, b = sets.rng("f")
+    P = _Proxy(sets.P, pos=_pad_slice(jitter(sets.view("f", "pos"), sigma_x), a, sets.P.n),
+               vel=_pad_slice(jitter(sets.view("f", "vel"), sigma_v), a, sets.P.n))
+    c, d = sets.rng("d")
+    D = sets.D
+    if d > c:
+        D = _Proxy(sets.D, pos=_pad_slice(jitter(sets.view("d", "pos"), sigma_x), c, sets.D.n),
+                   vel=_pad_slice(jitter(sets.view("d", "vel"), sigma_v), c, sets.D.n))
+    return Sets(P, sets.B, D, sets.W, f=sets.f, d=sets.d, b=sets.b, w=sets.w)
+
+
+def _pad_slice(t, start, n):
+    """A [n, ...] view-compatible tensor whose rows [start, start + len(t)) are t
+    (the other rows are never read)."""
+    out = torch.empty((n,) + tuple(t.shape[1:]), dtype=t.dtype, device=t.device)
+    out[start:start + t.shape[0]] = t
+    return out
+
+
 def train(net: Network, ts: TrainingSet, members, iters: int, lr: float = 1e-3, seed: int = 0, log=None,
-          log_every: int = 200) -> list:
-    """Adam on single-member samples drawn uniformly from the training set."""
+          log_every: int = 200, edge_weight: float = 0.0, noise: tuple = (0.0, 0.0), extra=None,
+          extra_fraction: float = 0.5) -> list:
+    """Adam on single-member samples drawn uniformly from the training set.
+    edge_weight > 0 adds the edge term (relative displacement errors of
+    neighbours, which is what the density judge sees) to the loss; noise =
+    (sigma_x [m], sigma_v [m/s]) perturbs the inputs (targets unchanged);
+    extra = [(sets, x_t, v_t), ...] samples (collect_on_policy) drawn with
+    probability extra_fraction."""
     rng = np.random.default_rng(seed)
+    gen = torch.Generator(device=net.device).manual_seed(seed)
     lib = net.lib
     g = Graph(net.cfg, net.device)
     hist = []
     t0 = time.perf_counter()
     for it in range(iters):
-        snap = ts.snapshots[int(rng.integers(len(ts.snapshots)))]
-        k = int(members[int(rng.integers(len(members)))])
-        sets, x_t, v_t = sample_sets(ts, snap, k)
+        if extra and rng.random() < extra_fraction:
+            sets, x_t, v_t = extra[int(rng.integers(len(extra)))]
+        else:
+            snap = ts.snapshots[int(rng.integers(len(ts.snapshots)))]
+            k = int(members[int(rng.integers(len(members)))])
+            sets, x_t, v_t = sample_sets(ts, snap, k)
+        if noise[0] > 0.0 or noise[1] > 0.0:
+            sets = _noisy(sets, noise[0], noise[1], gen)
         g.set_nodes(sets)
         g.build(check=(it % 50 == 0))
         prepare_target(lib, g, sets, x_t, v_t, net.cfg)
         g.forward(net, store_pre=True)
         L = g.loss()
+        if edge_weight > 0.0:
+            L = g.edge_loss(edge_weight)
         g.backward(net)
         cos = 0.5 * (1.0 + math.cos(math.pi * it / max(iters, 1)))
         net.adam(lr * (0.05 + 0.95 * cos))
