@@ -172,3 +172,23 @@ def test_adam_steps_reduce_the_loss_of_a_fixed_sample():
         net.adam(3e-3)
     assert losses[-1] < 0.5 * losses[0], losses[::10]
     assert int(g.status()) == 0
+
+
+def test_inference_forward_matches_training_forward():
+    """The inference pass forms the residuals while staging the next layer's
+    operand tile; the training pass stores them.  Same network, same output
+    (up to the order of the FP32 atomics at run boundaries)."""
+    from warp_sph_gpt_gb300.surrogate import Network
+
+    g, cfg, d = _synthetic(3)
+    net = Network(cfg, "cuda", seed=7)
+    th = net.theta.clone()
+    th[O.N3_W:O.N3_W + 6 * 128] *= 30.0
+    net.theta.copy_(th)
+    net.pack()
+    a = g.forward(net, store_pre=True).clone()
+    b = g.forward(net, store_pre=False).clone()
+    torch.cuda.synchronize()
+    assert int(g.status()) == 0
+    err = (a - b).abs().max().item() / max(a.abs().max().item(), 1e-30)
+    assert err <= 1e-3, err

@@ -153,8 +153,11 @@ __global__ void k_pack(const float* __restrict__ theta, uint16_t* __restrict__ p
 // ---------------------------------------------------------------------------
 // node MLP layers: out = epi(A[M,K] * B[N,K]^T + bias)
 // ---------------------------------------------------------------------------
+// add (optional, K = 128): rows r < n_add of the A operand are A[r] + add[r]
+// (the residual h + s * sum_j f_ij (.) h_j, formed while staging the tile).
 template <int K, int N, int EPI, bool IMG>
-__global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int M, const uint16_t* __restrict__ B,
+__global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int M, const float* __restrict__ add,
+                                             int n_add, const uint16_t* __restrict__ B,
                                              const float* __restrict__ bias, float* __restrict__ out_f32,
                                              uint16_t* __restrict__ out_bf, float* __restrict__ z_out,
                                              int32_t* status) {
@@ -189,10 +192,19 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
     constexpr uint32_t idesc = umma::idesc_bf16(128, N);
     for (int tile = blockIdx.x; !failed && tile * kT < M; tile += gridDim.x) {
         const int row = tile * kT + tid;
+        const bool plus = add != nullptr && row < n_add;
 #pragma unroll
         for (int q = 0; q < K / 8; ++q) {
             uint4 v = make_uint4(0, 0, 0, 0);
             if (row < M) v = __ldg(reinterpret_cast<const uint4*>(A + (size_t)row * K) + q);
+            if (plus) {
+                const float4 a0 = __ldg(reinterpret_cast<const float4*>(add + (size_t)row * K + 8 * q));
+                const float4 a1 = __ldg(reinterpret_cast<const float4*>(add + (size_t)row * K + 8 * q + 4));
+                v = make_uint4(pack2(bf((uint16_t)v.x) + a0.x, bf((uint16_t)(v.x >> 16)) + a0.y),
+                               pack2(bf((uint16_t)v.y) + a0.z, bf((uint16_t)(v.y >> 16)) + a0.w),
+                               pack2(bf((uint16_t)v.z) + a1.x, bf((uint16_t)(v.z >> 16)) + a1.y),
+                               pack2(bf((uint16_t)v.w) + a1.z, bf((uint16_t)(v.w >> 16)) + a1.w));
+            }
             *reinterpret_cast<uint4*>(sA + tile_off(tid, 8 * q, K)) = v;
         }
         operands_ready();
@@ -306,7 +318,8 @@ constexpr uint32_t kImg128 = 128 * 128 * 2;  // 32 KB
 constexpr uint32_t EF_IMG1 = 0, EF_IMG2 = EF_IMG1 + kImg16, EF_B1 = EF_IMG2 + kImg128, EF_B2 = EF_B1 + 512,
                    EF_BARS = EF_B2 + 512, EF_SLOT = EF_BARS + 48, EF_PIPE = (EF_SLOT + 16 + 1023) / 1024 * 1024,
                    EF_P_XS = 0, EF_P_ZR = EF_P_XS + kImg16, EF_P_SR = EF_P_ZR + kImg128, EF_P_SJ = EF_P_SR + 512,
-                   EF_P_H = EF_P_SJ + 512, EF_P_BYTES = EF_P_H + kImg128, EF_BYTES = EF_PIPE + 2 * EF_P_BYTES;
+                   EF_P_END = EF_P_SJ + 512, EF_P_H = EF_P_END + 16, EF_P_BYTES = EF_P_H + kImg128,
+                   EF_BYTES = EF_PIPE + 2 * EF_P_BYTES;
 static_assert(EF_PIPE % 1024 == 0 && EF_P_BYTES % 16 == 0 && EF_P_H % 16 == 0, "k_edges shared memory alignment");
 static_assert(EF_BYTES <= 227 * 1024, "k_edges shared memory");
 
@@ -454,7 +467,15 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
             umma::commit(bar);
         }
         if (loader) {
-            if (MODE == MODE_AGG && sj[lt] >= 0) tma_load_1d(hs + lt * 256, a.h + (size_t)sj[lt] * kH, 256, hbar);
+            if (MODE == MODE_AGG) {
+                if (sj[lt] >= 0) tma_load_1d(hs + lt * 256, a.h + (size_t)sj[lt] * kH, 256, hbar);
+                // edges after which the running sum is flushed: the last edge of a
+                // receiver's run, and the last valid edge of each half-tile
+                const int r = sr[lt];
+                const bool flush = r >= 0 && (lt == kT - 1 || lt == kT / 2 - 1 || sr[lt + 1] != r);
+                const unsigned m = __ballot_sync(0xffffffffu, flush);
+                if ((lt & 31) == 0) reinterpret_cast<uint32_t*>(pb + EF_P_END)[lt >> 5] = m;
+            }
             edge_load_ids(a, (tile + stride) * kT + lt, E, nxt);  // prefetch the next tile's ids
         }
         if (MODE == MODE_AGG) hpending = true;
@@ -506,24 +527,20 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
             hphase ^= 1u;
             hpending = false;
             const uint16_t* h16 = reinterpret_cast<const uint16_t*>(hs) + c;
+            const uint32_t* ends = reinterpret_cast<const uint32_t*>(pb + EF_P_END);
 #pragma unroll 1
             for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
                 float v[32];
                 umma::tmem_ld32(umma::taddr(tmem, lanes, c0), v);
+                const uint32_t em = ends[c0 >> 5];
 #pragma unroll
-                for (int i4 = 0; i4 < 32; i4 += 4) {
-                    const int4 r4 = *reinterpret_cast<const int4*>(sr + c0 + i4);
-                    const int rq[4] = {r4.x, r4.y, r4.z, r4.w};
-#pragma unroll
-                    for (int u = 0; u < 4; ++u) {
-                        const int i = i4 + u, rr = rq[u];
-                        if (rr < 0) continue;
-                        if (rr != cur) {
-                            if (cur >= 0) atomicAdd(a.agg + (size_t)cur * kH + c, acc * a.inv_norm);
-                            cur = rr;
-                            acc = 0.0f;
-                        }
-                        acc = fmaf(v[i] + bc, bf(h16[(c0 + i) * kH]), acc);
+                for (int i = 0; i < 32; ++i) {
+                    const float t = fmaf(v[i] + bc, bf(h16[(c0 + i) * kH]), acc);
+                    if (em & (1u << i)) {  // warp-uniform: the same edges end a run for every feature
+                        atomicAdd(a.agg + (size_t)sr[c0 + i] * kH + c, t * a.inv_norm);
+                        acc = 0.0f;
+                    } else {
+                        acc = t;
                     }
                 }
             }
@@ -544,7 +561,6 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
                 }
             }
         }
-        if (MODE == MODE_AGG && cur >= 0) atomicAdd(a.agg + (size_t)cur * kH + c, acc * a.inv_norm);
         umma::fence_before();
         pipe_sync256(bid);
     }
@@ -1137,14 +1153,14 @@ int smem_opt_in(Kern k, uint32_t bytes) {
 
 template <int K, int N, int EPI, bool IMG>
 int rows(const uint16_t* A, int M, const uint16_t* B, const float* bias, float* out_f32, uint16_t* out_bf,
-         float* z_out, int32_t* status, cudaStream_t st) {
+         float* z_out, int32_t* status, cudaStream_t st, const float* add = nullptr, int n_add = 0) {
     if (M <= 0) return SPHDEM_OK;
     constexpr uint32_t bytes = N * K * 2 + kT * K * 2 + 4 * (N < 2 ? 2 : N) + 16 + 16;
     int rc = smem_opt_in(k_rows<K, N, EPI, IMG>, bytes);
     if (rc) return rc;
     const int tiles = (M + kT - 1) / kT;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-    k_rows<K, N, EPI, IMG><<<grid, kT, bytes, st>>>(A, M, B, bias, out_f32, out_bf, z_out, status);
+    k_rows<K, N, EPI, IMG><<<grid, kT, bytes, st>>>(A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status);
     return launch_status("mpnn rows");
 }
 
@@ -1304,16 +1320,25 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
         a.agg = n->agg;
         if (nr > 0 && (rc = edges<MODE_AGG>(a, eg, st))) return rc;
         if (round == 0) {
-            k_residual<<<blocks_for((long)nn * 64, 256), 256, 0, st>>>(n->h0, n->agg, nr, nn, n->h1);
-            rc = rows<128, 128, EPI_SILU, true>(n->h1, nn, n->packed + P_N2, n->theta + SPHDEM_MPNN_N2_B, nullptr,
-                                                n->h2, store_pre ? n->z2 : nullptr, n->status, st);
+            if (store_pre) {  // the backward pass needs h1 itself
+                k_residual<<<blocks_for((long)nn * 64, 256), 256, 0, st>>>(n->h0, n->agg, nr, nn, n->h1);
+                rc = rows<128, 128, EPI_SILU, true>(n->h1, nn, n->packed + P_N2, n->theta + SPHDEM_MPNN_N2_B,
+                                                    nullptr, n->h2, n->z2, n->status, st);
+            } else {  // h1 = h0 + agg formed while staging
+                rc = rows<128, 128, EPI_SILU, true>(n->h0, nn, n->packed + P_N2, n->theta + SPHDEM_MPNN_N2_B,
+                                                    nullptr, n->h2, nullptr, n->status, st, n->agg, nr);
+            }
             if (rc) return rc;
-        } else {
+        } else if (store_pre) {
             k_residual<<<blocks_for((long)nr * 64, 256), 256, 0, st>>>(n->h2, n->agg, nr, nr, n->h3);
         }
     }
-    rc = rows<128, 16, EPI_F32, true>(n->h3, nr, n->packed + P_N3, n->theta + SPHDEM_MPNN_N3_B, n->out, nullptr,
-                                      nullptr, n->status, st);
+    if (store_pre)
+        rc = rows<128, 16, EPI_F32, true>(n->h3, nr, n->packed + P_N3, n->theta + SPHDEM_MPNN_N3_B, n->out, nullptr,
+                                          nullptr, n->status, st);
+    else
+        rc = rows<128, 16, EPI_F32, true>(n->h2, nr, n->packed + P_N3, n->theta + SPHDEM_MPNN_N3_B, n->out, nullptr,
+                                          nullptr, n->status, st, n->agg, nr);
     if (rc) return rc;
     return launch_status("mpnn_forward");
 }
