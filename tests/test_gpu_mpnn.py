@@ -192,3 +192,33 @@ def test_inference_forward_matches_training_forward():
     assert int(g.status()) == 0
     err = (a - b).abs().max().item() / max(a.abs().max().item(), 1e-30)
     assert err <= 1e-3, err
+
+
+def test_edge_loss_matches_its_formula():
+    """lambda / E * sum over edges (i <- j) of |dx_i - dx_j|^2, dx_j = 0 for
+    senders that are not receivers; gradient added to d_out."""
+    g, cfg, d = _synthetic(5)
+    nr = d["n_recv"]
+    rng = np.random.default_rng(1)
+    out = rng.normal(0, 1, (nr, 16)).astype(np.float32)
+    tgt = rng.normal(0, 1, (nr, 16)).astype(np.float32)
+    g.buf["out"][:nr] = torch.tensor(out, device="cuda")
+    t = torch.tensor(tgt, device="cuda")
+    g.loss(t)
+    base_loss = g.buf["loss"].item()
+    base_grad = g.buf["d_out"][:nr].cpu().numpy().copy()
+    lam = 0.7
+    total = g.edge_loss(lam, t).item()
+    grad = g.buf["d_out"][:nr].cpu().numpy()
+    snd, rcv = _oracle_edges(g, d)
+    dx = out[:, :3].astype(np.float64) - tgt[:, :3]
+    dj = np.where((snd < nr)[:, None], dx[np.minimum(snd, nr - 1)], 0.0)
+    diff = dx[rcv] - dj
+    E = len(snd)
+    ref = lam / E * (diff * diff).sum()
+    assert abs((total - base_loss) - ref) <= 1e-4 * ref
+    gref = np.zeros((nr, 16))
+    np.add.at(gref[:, :3], rcv, 2 * lam / E * diff)
+    m = snd < nr
+    np.add.at(gref[:, :3], snd[m], -2 * lam / E * diff[m])
+    np.testing.assert_allclose(grad - base_grad, gref, rtol=1e-4, atol=1e-7)

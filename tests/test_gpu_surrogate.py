@@ -7,6 +7,8 @@
   one-jump error (mean squared normalised residual over the K = 10 step jump)
   is well below that of the constant-acceleration prior alone (the surrogate
   with its output set to zero).
+* On-policy samples pair the states a judged learned rollout visits with the
+  plain method's continuation from them.
 * A rollout of the config-1 dam break with the plain-step fallback keeps its
   accounting (every jump accepted or undone), stays finite, and never accepts
   a jump whose density moved by more than the judge's tolerance.
@@ -44,6 +46,24 @@ def test_trained_network_beats_the_prior_on_held_out_members(trained):
     assert np.isfinite(val)
     assert 0.5 < prior < 2.0  # output scales are the prior's RMS residual
     assert val < 0.6 * prior
+
+
+def test_on_policy_samples_pair_rollout_states_with_plain_targets(trained):
+    """collect_on_policy: one sample per jump window of each case, the target is
+    the plain continuation, and training on them keeps the loss finite."""
+    from warp_sph_gpt_gb300.batch import Case
+    from warp_sph_gpt_gb300.generate import config_batch_member
+    from warp_sph_gpt_gb300.surrogate import collect_on_policy, train
+
+    picks = [m for m in (config_batch_member(1000 + i) for i in range(1, 12)) if len(m[1])][:2]
+    cases = [Case(*m) for m in picks]
+    samples = collect_on_policy(trained["net"], cases, 100)
+    assert len(samples) == 10 * len(cases)
+    for sets, x_t, v_t in samples:
+        assert x_t.shape == v_t.shape == (sets.P.n + sets.D.n, 3)
+        assert torch.isfinite(x_t).all() and torch.isfinite(v_t).all()
+    hist = train(trained["net"], trained["ts"], list(range(6)), iters=50, lr=1e-4, extra=samples, log_every=10)
+    assert all(np.isfinite(h[1]) for h in hist)
 
 
 def test_rollout_with_fallback_respects_the_judge(trained):
