@@ -261,6 +261,42 @@ def porosity_compute_roofline(ctx, D, scales, porosity_ms: float, device):
             "peak_basis": f"{props.multi_processor_count} SMs x 128 FP32 lanes x {mhz:.0f} MHz"}
 
 
+def output_run(args, solv, P, B, D, W, grids, scales, n_units, first_step):
+    """The same steps with a VTP frame (fluid + wall, DEM) every output_step
+    steps through the asynchronous FrameWriter; wall time includes writing every
+    file and the collections."""
+    import shutil
+    import tempfile
+
+    import torch
+
+    from warp_sph_gpt_gb300 import run_steps
+    from warp_sph_gpt_gb300.output import FrameWriter
+
+    out_dir = tempfile.mkdtemp(prefix="sphdem_frames_")
+    try:
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        writer = FrameWriter(solv, P, B, D, W, out_dir=out_dir)
+        step = first_step
+        for _ in range(max(1, args.steps // args.output_step)):
+            run_steps(solv, P, B, grids[0], grids[1], D, W, grids[2], grids[3], first_step=step,
+                      n_steps=args.output_step, search_scales=scales)
+            step += args.output_step
+            writer.write_frame(step)
+        writer.finalize()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+        files = os.listdir(out_dir)
+        size = sum(os.path.getsize(os.path.join(out_dir, f)) for f in files)
+        steps = step - first_step
+        return {"value": n_units * steps / wall, "unit": "particle-steps/s", "steps": steps,
+                "frames": len(writer.frames), "bytes_written": size, "wall_s": round(wall, 3),
+                "note": "wall clock incl. formatting and writing every VTP/PVD file (asynchronous writer thread)"}
+    finally:
+        shutil.rmtree(out_dir, ignore_errors=True)
+
+
 def job_throughput(units_per_replica: int, steps: int, world: int, ms_max: float) -> float:
     """Whole-job particle-steps/s of `world` replicas timed by the slowest."""
     return world * units_per_replica * steps / (ms_max * 1e-3)
@@ -353,6 +389,8 @@ def gpu_arm(args, rank, world, local_rank):
     achieved = alg_bytes / (phases[dom] * 1e-3) / 1e9 if phases[dom] > 0 else 0.0
 
     compute = porosity_compute_roofline(ctx, D, scales, phases.get("porosity", 0.0), device)
+    output = output_run(args, solv, P, B, D, W, grids, scales, n_units, first + args.steps + reps) \
+        if args.output_step > 0 else None
 
     # e2e through the public API with host buffers
     e2e_steps = min(args.steps, args.e2e_steps)
@@ -410,6 +448,7 @@ def gpu_arm(args, rank, world, local_rank):
                      "algorithmic_bytes_per_launch": alg_bytes,
                      "traffic": profile_traffic(dom, args.workload)},
         "compute_roofline": compute,
+        "with_output": output,
         "phases_ms": phases,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
@@ -742,6 +781,8 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-budget-s", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--output-step", type=int, default=0,
+                    help="also time the run with a VTP frame every N steps (asynchronous writer)")
     ap.add_argument("--porosity-variant", type=int, default=-1, choices=(-1, 0, 1),
                     help="porosity normaliser implementation (-1 = library default)")
     ap.add_argument("--lanes-sph", type=int, default=0, choices=(0, 1, 32),

@@ -375,6 +375,18 @@ int sphdem_neighbour_digest(sphdem_ctx_t* c, int relation, float radius,
  * double[8]. */
 int sphdem_diagnostics(sphdem_ctx_t* c, float g, double* out, sphdem_stream_t s);
 
+/* ---- frame output (host) -------------------------------------------------
+ * ASCII formatting of VTK XML PolyData arrays as output/output.py:16-25
+ * (_fmt_float / _fmt_int) writes them: "%.6g" of each float as a double, or
+ * "%d", one space between values, per_line values per line, lines joined by
+ * '\n', no trailing newline.  Split over `threads` host threads (0 = all) by
+ * whole lines; the text does not depend on the thread count.  out == NULL
+ * returns the byte count; otherwise the bytes written, -1 if cap is too small,
+ * -2 for invalid arguments. */
+int64_t sphdem_format_f32(const float* v, int64_t n, int32_t per_line, char* out, int64_t cap, int32_t threads);
+int64_t sphdem_format_i32(const int32_t* v, int64_t n, int32_t per_line, char* out, int64_t cap,
+                          int32_t threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -159,6 +159,8 @@ _SIGNATURES = {
     "sphdem_neighbour_digest": ([C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p],
                                 C.c_int),
     "sphdem_diagnostics": ([C.c_void_p, C.c_float, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_format_f32": ([C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32], C.c_int64),
+    "sphdem_format_i32": ([C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32], C.c_int64),
     # include/sphdem_mpnn.h
     "sphdem_mpnn_partial_floats": ([], C.c_int64),
     "sphdem_mpnn_pack": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
