@@ -7,10 +7,11 @@ and fixed DEM spheres (``dem_XXXXXX.vtp``), tied into ``sph.pvd`` /
 ``dem.pvd`` time series.  Byte-identical text (tests/test_output.py).
 
 GB300 side: ``FrameWriter.write_frame`` does not stall the step loop.  It
-orders a copy of the frame's fields into pinned host buffers on a side CUDA
-stream (after the work queued so far on the step stream) and returns; a host
-thread waits for the copy, checks the fields are finite, formats the arrays
-with the library's multi-threaded "%.6g" formatter and writes the files.  A
+snapshots the frame's fields device-to-device on the step stream (HBM speed),
+orders their copy into pinned host buffers on a side CUDA stream, and returns;
+a host thread waits for that copy, checks the fields are finite, formats the
+arrays with the library's multi-threaded "%.6g" formatter and writes the
+files.  A
 small ring of pinned buffers bounds the frames in flight.  A non-finite field
 raises ``FloatingPointError`` (as the reference does) at the next
 ``write_frame`` or at ``finalize``, and that frame's files are not written.
@@ -140,14 +141,16 @@ def save_pvd(frames, out_dir: str, name: str = "ptl") -> str:
 
 
 class _Slot:
-    """Pinned host copies of every field one frame needs."""
+    """Device staging and pinned host copies of every field one frame needs."""
 
     def __init__(self, parts):
-        self.host = {}
+        self.host, self.dev = {}, {}
         for kind, part, names in parts:
             for name in names:
                 t = getattr(part, name)
                 self.host[(kind, name)] = torch.empty(t.shape, dtype=t.dtype, pin_memory=t.is_cuda)
+                if t.is_cuda:
+                    self.dev[(kind, name)] = torch.empty_like(t)
         self.event = None
 
     def arrays(self, kind, names):
@@ -185,11 +188,16 @@ class FrameWriter:
         slot = self.free.get()  # blocks only when every buffer is in flight
         t = step * self.solv.dt
         if self.cuda:
-            self.stream.wait_stream(torch.cuda.current_stream(self.stream.device))
+            # device-to-device snapshot on the step stream (fast, so the run goes
+            # on at once), then the host copy on the side stream
+            main = torch.cuda.current_stream(self.stream.device)
+            for kind, part, names in self.parts:
+                for name in names:
+                    slot.dev[(kind, name)].copy_(getattr(part, name), non_blocking=True)
+            self.stream.wait_stream(main)
             with torch.cuda.stream(self.stream):
-                for kind, part, names in self.parts:
-                    for name in names:
-                        slot.host[(kind, name)].copy_(getattr(part, name), non_blocking=True)
+                for key, dev in slot.dev.items():
+                    slot.host[key].copy_(dev, non_blocking=True)
                 slot.event = torch.cuda.Event()
                 slot.event.record(self.stream)
         else:
