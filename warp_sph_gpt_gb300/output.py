@@ -46,14 +46,23 @@ def _fmt(a: np.ndarray, per_line: int, integer: bool) -> bytes:
     a = np.ascontiguousarray(a, dtype=np.int32 if integer else np.float32)
     fn = lib.sphdem_format_i32 if integer else lib.sphdem_format_f32
     n = a.size
-    size = fn(a.ctypes.data, n, per_line, None, 0, 0)
-    if size < 0:
-        raise ValueError("frame formatting failed")
-    buf = C.create_string_buffer(int(size))
-    got = fn(a.ctypes.data, n, per_line, buf, size, 0)
-    if got != size:
+    cap = 16 * n + 16  # "%.6g" of a float or "%d" of an int32 plus a separator fits 16 bytes
+    buf = C.create_string_buffer(cap)
+    got = fn(a.ctypes.data, n, per_line, buf, cap, 0)
+    if got < 0:
         raise RuntimeError("frame formatting failed")
     return buf.raw[:got]
+
+
+_VERTS: dict = {}
+
+
+def _verts(n: int) -> bytes:
+    """Connectivity and offsets text of n vertex cells (the same every frame)."""
+    if n not in _VERTS:
+        _VERTS.clear()
+        _VERTS[n] = (_fmt(np.arange(n, dtype=np.int32), 20, True), _fmt(np.arange(1, n + 1, dtype=np.int32), 20, True))
+    return _VERTS[n]
 
 
 def fmt_float(a, per_line: int = 6) -> str:
@@ -107,9 +116,9 @@ def vtp_bytes(d: dict, scalar: str) -> bytes:
              b'        <DataArray type="Float32" Name="Points" NumberOfComponents="3" format="ascii">\n',
              _fmt(d["pos"], 6, False), b"\n", b'        </DataArray>\n', b'      </Points>\n', b'      <Verts>\n',
              b'        <DataArray type="Int32" Name="connectivity" format="ascii">\n',
-             _fmt(np.arange(n, dtype=np.int32), 20, True), b"\n", b'        </DataArray>\n',
+             _verts(n)[0], b"\n", b'        </DataArray>\n',
              b'        <DataArray type="Int32" Name="offsets" format="ascii">\n',
-             _fmt(np.arange(1, n + 1, dtype=np.int32), 20, True), b"\n", b'        </DataArray>\n',
+             _verts(n)[1], b"\n", b'        </DataArray>\n',
              b'      </Verts>\n', f'      <PointData Scalars="{scalar}" Vectors="vel">\n'.encode()]
     for key, values in d.items():
         if key == "pos":
