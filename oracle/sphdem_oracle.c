@@ -78,8 +78,10 @@ static void* par_worker(void* arg) {
     return NULL;
 }
 
-/* Timing samples only: subjects i with i % g_stride != 0 are skipped, so a
-   step costs ~1/g_stride of the full work (results are then incomplete). */
+/* Timing samples only: ceil(n / g_stride) subjects are processed, a
+   pseudo-random scatter (k * 1000003) mod n of the index range, so a step
+   costs ~1/g_stride of the full work without aliasing with the lattice order
+   of the particles (results are then incomplete). */
 static int g_stride = 1;
 
 int oracle_set_subject_stride(int s) {
@@ -90,18 +92,19 @@ int oracle_set_subject_stride(int s) {
 typedef struct {
     body_fn fn;
     void* ctx;
+    int n;
 } strided_ctx;
 
 static void strided_body(void* c, int i) {
     strided_ctx* s = (strided_ctx*)c;
-    s->fn(s->ctx, i * g_stride);
+    s->fn(s->ctx, (int)(((long long)i * 1000003LL) % s->n));
 }
 
 static void par_for_all(int n, body_fn fn, void* ctx);
 
 static void par_for(int n, body_fn fn, void* ctx) {
     if (g_stride > 1) {
-        strided_ctx s = {fn, ctx};
+        strided_ctx s = {fn, ctx, n};
         par_for_all((n + g_stride - 1) / g_stride, strided_body, &s);
         return;
     }
