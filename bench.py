@@ -677,30 +677,49 @@ def _oracle_state(parts):
 
 
 def cpu_sample(host, solv, scales, stride: int, step: int) -> float:
+    """Seconds of one oracle step over every stride-th subject, run on a fresh
+    copy of the state (a sampled step leaves the unsampled subjects stale, so
+    samples must not run on each other's results)."""
+    import copy
+
     from oracle import oracle as O
 
+    state = copy.deepcopy(host)
     O.set_subject_stride(stride)
     t0 = time.perf_counter()
-    host.sphdem_onestep(solv, step, scales, p="f32")
+    state.sphdem_onestep(solv, step, scales, p="f32")
     dt = time.perf_counter() - t0
     O.set_subject_stride(1)
     return dt
 
 
+def _prime_at_least(k: int) -> int:
+    """Smallest prime >= k: prime strides do not alias with the particle
+    lattice's dimensions (every layer of the lattice is sampled alike)."""
+    k = max(2, int(k))
+    while any(k % d == 0 for d in range(2, int(k ** 0.5) + 1)):
+        k += 1
+    return k
+
+
 def cpu_fit(host, solv, scales, budget_s: float):
-    """Choose a subject stride S so one sample fits the budget, then fit the
-    full-step time F + V from samples at S and 2S."""
+    """Choose a prime subject stride S so one sample fits the budget, then fit
+    the full-step time F + V from samples at S and at a prime near 2S."""
     n = len(host.sph["pos"])
-    stride = max(1, n // 2048)
+    stride = _prime_at_least(max(2, n // 2048))
     t = cpu_sample(host, solv, scales, stride, 1)
     # aim one sample at ~budget/4
-    while t < budget_s / 8 and stride > 1:
-        stride = max(1, stride // 2)
+    while t < budget_s / 8 and stride > 2:
+        stride = _prime_at_least(max(2, stride // 2))
         t = cpu_sample(host, solv, scales, stride, 1)
+        if stride == 2:
+            break
+    s2 = _prime_at_least(2 * stride)
     t1 = cpu_sample(host, solv, scales, stride, 1)
-    t2 = cpu_sample(host, solv, scales, 2 * stride, 1) if stride * 2 <= n else t1
-    V = max(0.0, 2 * stride * (t1 - t2)) if stride > 1 else t1
-    F = max(0.0, t1 - V / stride)
+    t2 = cpu_sample(host, solv, scales, s2, 1) if s2 <= n else t1
+    inv1, inv2 = 1.0 / stride, 1.0 / s2
+    V = max(0.0, (t1 - t2) / (inv1 - inv2)) if t1 > t2 else t1 * stride
+    F = max(0.0, t1 - V * inv1)
     return stride, t1, t2, F + V
 
 
@@ -714,8 +733,9 @@ def cpu_baseline(gen, solv, parts, scales, budget_s):
     n_units = len(host.sph["pos"]) + len(host.dem["pos"])
     return {"value": n_units / full, "unit": "particle-steps/s", "cores": cores, "kind": "port",
             "sample": f"CPU oracle (restatement of the reference Warp kernels, FP32) on {cores} threads: one coupled "
-                      f"step on every {stride}-th and every {2 * stride}-th subject particle ({t1:.2f} s, {t2:.2f} s), "
-                      f"full step {full:.2f} s from the fit t(S) = F + V/S"}
+                      f"step on every {stride}-th and every {_prime_at_least(2 * stride)}-th subject particle "
+                      f"({t1:.2f} s, {t2:.2f} s; prime strides, a fresh copy of the state per sample), full step "
+                      f"{full:.2f} s from the fit t(S) = F + V/S"}
 
 
 def reference_arm(args):

@@ -78,10 +78,11 @@ static void* par_worker(void* arg) {
     return NULL;
 }
 
-/* Timing samples only: ceil(n / g_stride) subjects are processed, a
-   pseudo-random scatter (k * 1000003) mod n of the index range, so a step
-   costs ~1/g_stride of the full work without aliasing with the lattice order
-   of the particles (results are then incomplete). */
+/* Timing samples only: subjects i with i % g_stride != 0 are skipped, so a
+   step costs ~1/g_stride of the full work (results are then incomplete).  The
+   sampled subjects stay close to each other, so their neighbourhoods share
+   caches as in a full pass; callers pick a stride coprime to the particle
+   lattice's dimensions so the sample does not alias with its layers. */
 static int g_stride = 1;
 
 int oracle_set_subject_stride(int s) {
@@ -92,19 +93,18 @@ int oracle_set_subject_stride(int s) {
 typedef struct {
     body_fn fn;
     void* ctx;
-    int n;
 } strided_ctx;
 
 static void strided_body(void* c, int i) {
     strided_ctx* s = (strided_ctx*)c;
-    s->fn(s->ctx, (int)(((long long)i * 1000003LL) % s->n));
+    s->fn(s->ctx, i * g_stride);
 }
 
 static void par_for_all(int n, body_fn fn, void* ctx);
 
 static void par_for(int n, body_fn fn, void* ctx) {
     if (g_stride > 1) {
-        strided_ctx s = {fn, ctx, n};
+        strided_ctx s = {fn, ctx};
         par_for_all((n + g_stride - 1) / g_stride, strided_body, &s);
         return;
     }
