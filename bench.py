@@ -483,6 +483,8 @@ def _edge_flops(E, nn, nr):
 
 
 def learned_arm(args, rank, world, local_rank):
+    import ctypes as C
+
     import torch
 
     from warp_sph_gpt_gb300 import surrogate as S
@@ -574,7 +576,7 @@ def learned_arm(args, rank, world, local_rank):
     ro.run(0, 6 * K)  # both Shepard variants run eagerly once, then are captured
     torch.cuda.synchronize()
     learned.restore(snapL)
-    ro.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0)
+    ro.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0, jump_kernels=0)
     # e2e: initial state from pinned host memory, final state back to the host
     host_in = {k: t.detach().cpu().pin_memory() for k, t in (("pos", learned.P.pos), ("vel", learned.P.vel),
                                                               ("dpos", learned.D.pos), ("dvel", learned.D.vel))}
@@ -661,7 +663,8 @@ def learned_arm(args, rank, world, local_rank):
                 "d2h_bytes_per_step": h2d / n,
                 "api": "LearnedRollout.run over the whole rollout; initial state from pinned host memory, final "
                        "state back"},
-        "gpu_launches": None,
+        "gpu_launches": stats["jump_kernels"] + (stats["plain_steps"] - stats["jumps"])
+        * max(0, int(ro.lib.sphdem_graph_kernels(C.byref(ro.ctx.ctx), 0))),
         "clocks": clocks_learned.summary(),
         "wall_s": round(time.perf_counter() - t_start, 1),
     }

@@ -198,6 +198,10 @@ typedef struct sphdem_jump {
 int sphdem_jump(sphdem_ctx_t* ctx, const sphdem_params_t* p, const sphdem_jump_t* j, int step,
                 sphdem_stream_t stream);
 
+/* Kernel nodes of the jump's captured graph (variant 1: Shepard step), or -1
+ * if that variant has not been captured yet. */
+int sphdem_jump_kernels(sphdem_ctx_t* ctx, int variant);
+
 /* Restore positions, velocities and fluid density saved by the last jump. */
 int sphdem_jump_undo(sphdem_ctx_t* ctx, const sphdem_jump_t* j, sphdem_stream_t stream);
 

@@ -182,6 +182,7 @@ _SIGNATURES = {
                           C.c_void_p], C.c_int),
     "sphdem_jump": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
     "sphdem_jump_undo": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "sphdem_jump_kernels": ([C.c_void_p, C.c_int], C.c_int),
     "sphdem_mpnn_wgrad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,
                            C.c_void_p], C.c_int),
 }

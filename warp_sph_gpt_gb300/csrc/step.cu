@@ -214,6 +214,22 @@ int loop_body(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, int coupled,
     return sph_onestep(c, p, shep, true, st);
 }
 
+int count_kernel_nodes(cudaGraph_t graph) {
+    size_t n_nodes = 0;
+    cudaGraphGetNodes(graph, nullptr, &n_nodes);
+    int n_kernels = 0;
+    if (n_nodes) {
+        cudaGraphNode_t* nodes = new cudaGraphNode_t[n_nodes];
+        cudaGraphGetNodes(graph, nodes, &n_nodes);
+        for (size_t i = 0; i < n_nodes; ++i) {
+            cudaGraphNodeType t;
+            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++n_kernels;
+        }
+        delete[] nodes;
+    }
+    return n_kernels;
+}
+
 int capture(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, int coupled, GraphEntry& e) {
     cudaError_t err = cudaStreamBeginCapture(e.cap, cudaStreamCaptureModeThreadLocal);
     if (err != cudaSuccess) {
@@ -231,19 +247,7 @@ int capture(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, int coupled, G
         set_error("graph capture end", err);
         return SPHDEM_ERR_CUDA;
     }
-    size_t n_nodes = 0;
-    cudaGraphGetNodes(graph, nullptr, &n_nodes);
-    int n_kernels = 0;
-    if (n_nodes) {
-        cudaGraphNode_t* nodes = new cudaGraphNode_t[n_nodes];
-        cudaGraphGetNodes(graph, nodes, &n_nodes);
-        for (size_t i = 0; i < n_nodes; ++i) {
-            cudaGraphNodeType t;
-            if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++n_kernels;
-        }
-        delete[] nodes;
-    }
-    e.kernels[shep ? 1 : 0] = n_kernels;
+    e.kernels[shep ? 1 : 0] = count_kernel_nodes(graph);
     err = cudaGraphInstantiate(&e.exec[shep ? 1 : 0], graph, 0);
     cudaGraphDestroy(graph);
     if (err != cudaSuccess) {
@@ -532,6 +536,7 @@ struct JumpEntry {
     cudaStream_t cap = nullptr;
     cudaGraphExec_t exec[2] = {nullptr, nullptr};
     bool warm[2] = {false, false};
+    int kernels[2] = {0, 0};
 };
 std::map<const sphdem_ctx_t*, JumpEntry> g_jumps;
 
@@ -588,6 +593,7 @@ int sphdem_jump(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* 
             set_error("jump capture end", err);
             return SPHDEM_ERR_CUDA;
         }
+        e.kernels[v] = count_kernel_nodes(graph);
         err = cudaGraphInstantiate(&e.exec[v], graph, 0);
         cudaGraphDestroy(graph);
         if (err != cudaSuccess) {
@@ -601,6 +607,13 @@ int sphdem_jump(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* 
         return SPHDEM_ERR_CUDA;
     }
     return SPHDEM_OK;
+}
+
+int sphdem_jump_kernels(sphdem_ctx_t* c, int variant) {
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    auto it = g_jumps.find(c);
+    if (it == g_jumps.end() || !it->second.exec[variant ? 1 : 0]) return -1;
+    return it->second.kernels[variant ? 1 : 0];
 }
 
 int sphdem_jump_undo(sphdem_ctx_t* c, const sphdem_jump_t* j, sphdem_stream_t stream) {
@@ -678,6 +691,13 @@ int sphdem_graph_kernels(sphdem_ctx_t* c, int variant) {
 
 int sphdem_release(sphdem_ctx_t* c) {
     std::lock_guard<std::mutex> lock(g_graph_mu);
+    auto jt = g_jumps.find(c);
+    if (jt != g_jumps.end()) {
+        for (auto& x : jt->second.exec)
+            if (x) cudaGraphExecDestroy(x);
+        if (jt->second.cap) cudaStreamDestroy(jt->second.cap);
+        g_jumps.erase(jt);
+    }
     auto it = g_graphs.find(c);
     if (it == g_graphs.end()) return SPHDEM_OK;
     drop_entry(it->second);

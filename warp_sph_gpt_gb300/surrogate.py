@@ -627,7 +627,8 @@ class LearnedRollout:
         self.dev = torch.zeros(1, dtype=torch.float32, device=net.device)
         self.host = torch.zeros(3, dtype=torch.float32).pin_memory()
         self.jump = None
-        self.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0)
+        self.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0,
+                          jump_kernels=0)
 
     def _setup(self) -> None:
         c, g = self.case, self.g
@@ -667,6 +668,8 @@ class LearnedRollout:
             ctx.set_params(c.solv, c.scales)
             _lib.check(lib.sphdem_jump(C.byref(ctx.ctx), C.byref(ctx.params), C.byref(self.jump), step, st),
                        "sphdem_jump")
+            shep = step == 0 or (c.solv.shepard_step > 0 and step % c.solv.shepard_step == 0)
+            self.stats["jump_kernels"] += max(0, int(lib.sphdem_jump_kernels(C.byref(ctx.ctx), int(shep))))
             D._flip("dem")  # the plain step of the jump swapped both contact CSRs
             D._flip("bnd")
             self.host[0:1].copy_(self.dev, non_blocking=True)
