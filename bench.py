@@ -223,11 +223,11 @@ def reduce_max(value: float, world: int, device=None) -> float:
     return float(t.item())
 
 
-# FP32 operations per candidate of the porosity normaliser's inner loop
-# (csrc/coupling.cu ball_weight + accumulate: 3 sub, 1 mul + 2 fma for d2,
-# 1 mul by 1/h^2, 1 fma + 1 max for u, 2 mul for u^4, 1 fma for 1 + 2q, 1 mul,
-# 1 fma into the sum), plus one MUFU square root.
-POROSITY_FP32_OPS_PER_PAIR = 14
+# FP32 instructions per candidate of the porosity normaliser's inner loop
+# (csrc/coupling.cu ball_weight_h + accumulate on the scaled copy: 3 sub,
+# 1 mul + 2 fma for s = q^2, 1 min, 4 fma for the Wendland polynomial, 1 fma
+# into the sum) plus one MUFU square root.
+POROSITY_FP32_OPS_PER_PAIR = 13
 
 
 def porosity_compute_roofline(ctx, D, scales, porosity_ms: float, device):

@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPHDEM_ABI_VERSION 7
+#define SPHDEM_ABI_VERSION 8
 
 /* ---- return codes ---------------------------------------------------- */
 #define SPHDEM_OK                0
@@ -172,7 +172,8 @@ typedef struct sphdem_ctl {
     int32_t e_dem;      /* directed DEM-DEM contacts of the last rebuild        */
     int32_t e_bnd;      /* directed DEM-wall contacts of the last rebuild       */
     int32_t n_near;     /* fluid particles with a DEM inside its coupling reach */
-    int32_t pad[9];
+    int32_t near_next;  /* next near-list entry to hand out (porosity pass 2)   */
+    int32_t pad[8];
 } sphdem_ctl_t;
 
 /* Sorted working copies (all device, all [n] in the order of their grid).

@@ -54,7 +54,7 @@ class GridT(C.Structure):
 
 class CtlT(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("step", "old_dem", "old_bnd", "status", "e_dem", "e_bnd",
-                                         "n_near")] + [("pad", C.c_int32 * 9)]
+                                         "n_near", "near_next")] + [("pad", C.c_int32 * 8)]
 
 
 class WorkT(C.Structure):
@@ -119,7 +119,7 @@ FLAG_CSR_DEM_OVERFLOW = 0x1
 FLAG_CSR_BND_OVERFLOW = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_TIMEOUT = 0x10
-ABI_VERSION = 7
+ABI_VERSION = 8
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
 REL = dict(SPH_SPH_SUPPORT=0, SPH_BND_SUPPORT=1, BND_SPH_SUPPORT=2, BND_BND_SUPPORT=3, SPH_SPH_FORCE=4,

@@ -72,30 +72,34 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     return r;
 }
 
-// V_j u^4 (1 + 2q) of one candidate, u = max(1 - q/2, 0): the Wendland
-// weight vanishes at q = 2 and is clamped to 0 beyond, so candidates outside
-// the ball contribute nothing and no membership branch or select is needed
-// (warps walk 32 different candidates; a branch would diverge).  A pair whose
-// membership the reference decides by its rounded length(r) < 2h lies, if
-// near that boundary, within a few ulps of q = 2, where u^4 ~ 1e-28: the
-// normaliser's value is the same (the neighbour sets themselves are checked
-// with the exact predicate elsewhere).  The factor 21/(16 pi h^3) is applied
-// by the caller once per sum.
+// V_j u^4 (1 + 2q) of one candidate (u = 1 - q/2), evaluated as the
+// expanded polynomial  1 + s (-5/2 + q (5/2 + q (-15/16 + q/8))),  s = q^2,
+// with s clamped to 4: one multiply fewer per candidate than the factored
+// form, and the weight vanishes at q = 2 (every Horner step is exact there),
+// so candidates beyond the ball add ~0 (|W| <= a few ulps of 1) and no
+// membership branch or select is needed (warps walk 32 different candidates;
+// a branch would diverge).  A pair whose membership the reference decides by
+// its rounded length(r) < 2h lies, if near that boundary, within a few ulps
+// of q = 2, where the weight is below 1e-6: the normaliser's value is the
+// same to FP32 rounding (the neighbour sets themselves are checked with the
+// exact predicate elsewhere).  The factor 21/(16 pi h^3) is applied by the
+// caller once per sum.
+__device__ __forceinline__ float wendland_poly(float s) {
+    s = fminf(s, 4.0f);
+    const float q = sqrt_approx(s);
+    const float c = fmaf(fmaf(fmaf(0.125f, q, -0.9375f), q, 2.5f), q, -2.5f);
+    return fmaf(c, s, 1.0f);
+}
+
 __device__ __forceinline__ float ball_weight(float px, float py, float pz, const float4& q, float ih2) {
     const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
-    const float qq = sqrt_approx(fmaf(dz, dz, fmaf(dy, dy, dx * dx)) * ih2);  // q = r / h
-    const float u = fmaxf(fmaf(-0.5f, qq, 1.0f), 0.0f);
-    const float u2 = u * u;
-    return q.w * ((u2 * u2) * fmaf(2.0f, qq, 1.0f));
+    return q.w * wendland_poly(fmaf(dz, dz, fmaf(dy, dy, dx * dx)) * ih2);
 }
 
 // The same for coordinates already in units of h (p and q scaled by 1/h).
 __device__ __forceinline__ float ball_weight_h(float px, float py, float pz, const float4& q) {
     const float dx = px - q.x, dy = py - q.y, dz = pz - q.z;
-    const float qq = sqrt_approx(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
-    const float u = fmaxf(fmaf(-0.5f, qq, 1.0f), 0.0f);
-    const float u2 = u * u;
-    return q.w * ((u2 * u2) * fmaf(2.0f, qq, 1.0f));
+    return q.w * wendland_poly(fmaf(dz, dz, fmaf(dy, dy, dx * dx)));
 }
 
 // Porosity pass 1: dry particles get clamp(1); the rest are listed.  The list
@@ -153,16 +157,46 @@ __device__ __forceinline__ float warp_fluid_sum(const CplArgs& a, int inst, floa
     return warp_sum(acc) * kaux.y;
 }
 
+// Solid fraction of a listed particle: the DEM neighbours within 2 h_b, each
+// V_b W(r, h_b) / normaliser (Kernel_prep_sphdem :89-108).  flt is the uniform
+// normaliser; without a uniform h each DEM in reach has its own sum.
+template <bool UNIFORM>
+__device__ __forceinline__ float porosity_solid(const CplArgs& a, const float4& p, int inst, float flt) {
+    float solid = 0.0f;
+    const Win w = window(a.gd, p.x, p.y, p.z, a.rq);
+    for_each_range(a.gd, w, inst, [&](int s, int e) {
+        for (int j = s; j < e; ++j) {  // warp-uniform loop over DEM candidates
+            const int b = a.gd.order[j];
+            const float3 pb = ld3(a.D.pos, b);
+            const D2 r = d2_exact(p.x, p.y, p.z, pb.x, pb.y, pb.z);
+            const float4 ab = a.aux[b];
+            if (r.d2 < ab.z) {
+                float local_flt = flt;
+                if (!UNIFORM) local_flt = warp_fluid_sum(a, inst, p.x, p.y, p.z, pad_radius(ab.w), ab.z, ab);
+                solid += a.D.volume[b] * w_aux(ab, fast_sqrt(r.d2)) / (local_flt + 1.0e-20f);
+            }
+        }
+    });
+    return solid;
+}
+
 // Porosity pass 2: one warp per listed particle.  UNIFORM: one DEM h for all
 // spheres (the normaliser is one sum per particle); otherwise each DEM in
-// reach has its own normaliser sum.
+// reach has its own normaliser sum.  Warps take list entries from a shared
+// counter (the work per entry varies with the fluid around it; a static
+// split leaves SMs idle at the end), so the warps resident together work on
+// consecutive entries (neighbours in space): they walk nearly the same
+// candidates in the same column order and share them through L1.  Which warp
+// takes an entry does not change its result.
 template <bool UNIFORM>
 __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
     const int lane = threadIdx.x & 31;
-    const int warps = gridDim.x * (blockDim.x >> 5);
     const int n_near = a.ctl->n_near;
-    const float4 kuni = make_float4(a.kern.inv_h, a.kern.cw, a.t_support, a.support);
-    for (int idx = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); idx < n_near; idx += warps) {
+    for (;;) {
+        int idx = 0;
+        if (lane == 0) idx = atomicAdd(&a.ctl->near_next, 1);
+        idx = __shfl_sync(0xffffffffu, idx, 0);
+        if (idx >= n_near) break;
         const int k = a.near_list[idx];
         const int o = a.gs.order[k];
         const float4 p = a.f_posv[k];
@@ -177,23 +211,9 @@ __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
 #pragma unroll 4
                 for (int j = s + lane; j < e; j += 32) acc += ball_weight_h(sx, sy, sz, a.f_posq[j]);
             });
-            flt = warp_sum(acc) * kuni.y;
+            flt = warp_sum(acc) * a.kern.cw;
         }
-        float solid = 0.0f;
-        const Win w = window(a.gd, p.x, p.y, p.z, a.rq);
-        for_each_range(a.gd, w, inst, [&](int s, int e) {
-            for (int j = s; j < e; ++j) {  // warp-uniform loop over DEM candidates
-                const int b = a.gd.order[j];
-                const float3 pb = ld3(a.D.pos, b);
-                const D2 r = d2_exact(p.x, p.y, p.z, pb.x, pb.y, pb.z);
-                const float4 ab = a.aux[b];
-                if (r.d2 < ab.z) {
-                    float local_flt = flt;
-                    if (!UNIFORM) local_flt = warp_fluid_sum(a, inst, p.x, p.y, p.z, pad_radius(ab.w), ab.z, ab);
-                    solid += a.D.volume[b] * w_aux(ab, fast_sqrt(r.d2)) / (local_flt + 1.0e-20f);
-                }
-            }
-        });
+        const float solid = porosity_solid<UNIFORM>(a, p, inst, flt);
         if (lane == 0) a.P.porosity[o] = fminf(fmaxf(1.0f - solid, a.eps_min), a.eps_max);
     }
 }
@@ -554,7 +574,7 @@ int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, f
     CplArgs a = make_args(c, support, h);
     a.eps_min = eps_min;
     a.eps_max = eps_max;
-    cudaError_t e = cudaMemsetAsync(&c->ctl->n_near, 0, sizeof(int), st);
+    cudaError_t e = cudaMemsetAsync(&c->ctl->n_near, 0, 2 * sizeof(int), st);  // n_near, near_next
     if (e != cudaSuccess) {
         set_error("porosity memset", e);
         return SPHDEM_ERR_CUDA;
