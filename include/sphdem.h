@@ -198,6 +198,13 @@ typedef struct sphdem_work {
     float* dem_aux;     /* [n_dem,4] 1/h, 21/(16 pi h^3), sqrt bound of 2h, 2h  */
     /* fluid, in grid_sph order, uniform DEM h only */
     float* f_posq;      /* [n_sph,4] x/h, y/h, z/h, m/rho (porosity sums)     */
+    /* fluid neighbour lists written by the density pass and read by the
+     * force pass of the same step, particles in grid_sph order, row-major by
+     * list position so a warp's reads coalesce: rows [0, cap) fluid slots,
+     * rows [cap, 2 cap) wall slots, row 2 cap the fluid count, row 2 cap + 1
+     * the wall count (a count above cap: that particle walks its cells).
+     * cap = params.nbr_cap; NULL or cap 0: no lists. */
+    int32_t* nbr;       /* [(2*cap+2), n_sph]                                  */
 } sphdem_work_t;
 
 /* Solver controls.  Reference: Solv (input/Config.py:11-49 with the SPH-DEM
@@ -229,7 +236,7 @@ typedef struct sphdem_params {
     int32_t block_sph;
     int32_t porosity_variant;
     int32_t lanes_sph;
-    int32_t pad_params;
+    int32_t nbr_cap;         /* neighbour-list capacity per particle (work.nbr) */
 } sphdem_params_t;
 
 /* Everything one step touches. */

@@ -72,3 +72,30 @@ def test_snapshot_restore_replays_bit_for_bit():
     torch.cuda.synchronize()
     for a, b in zip(first, (case.P.pos, case.P.vel, case.D.pos, case.D.omega)):
         np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+
+
+@pytest.mark.parametrize("nbr_cap", [0, 16])
+def test_neighbour_lists_give_identical_steps(nbr_cap):
+    """Forces from the density pass's neighbour lists equal the cell walk bit
+    for bit (same members, same order): lists off (0), and a capacity so small
+    that most particles overflow and walk (16), against the default lists."""
+    gen, _, _ = config_batch_member(4)
+    xs = np.arange(0.04, gen.fluid_width - 0.03, 0.07)
+    zs = np.arange(0.026, gen.fluid_height - 0.03, 0.07)
+    pos = np.array([(x, 0.2, z) for x in xs for z in zs])
+    rad = np.full(len(pos), 0.025)
+    ref = Case(gen, pos, rad)
+    ref.run(0, 25)
+    alt = Case(gen, pos, rad)
+    alt.tune({"nbr_cap": nbr_cap})
+    alt.run(0, 25)
+    torch.cuda.synchronize()
+    from warp_sph_gpt_gb300.engine import context_for
+
+    caps = [context_for(c.P, c.B, c.D, c.W, tuple(c.grids)).params.nbr_cap for c in (ref, alt)]
+    assert caps[0] >= 64 and caps[1] == nbr_cap
+    for part_a, part_b in ((ref.P, alt.P), (ref.D, alt.D)):
+        for field in ("pos", "vel"):
+            np.testing.assert_array_equal(getattr(part_a, field).cpu().numpy(), getattr(part_b, field).cpu().numpy())
+    np.testing.assert_array_equal(ref.P.acc.cpu().numpy(), alt.P.acc.cpu().numpy())
+    np.testing.assert_array_equal(ref.P.pgf.cpu().numpy(), alt.P.pgf.cpu().numpy())

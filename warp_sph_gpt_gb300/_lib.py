@@ -61,7 +61,8 @@ class WorkT(C.Structure):
     _fields_ = [("f_posm", c_float_p), ("f_vel", c_float_p), ("f_rp", c_float_p), ("f_vprev", c_float_p),
                 ("f_posv", c_float_p), ("f_pgf", c_float_p), ("near_list", c_int_p),
                 ("b_posm", c_float_p), ("b_vel", c_float_p), ("b_rp", c_float_p), ("b_vprev", c_float_p),
-                ("b_self", c_float_p), ("dem_count", c_int_p), ("dem_aux", c_float_p), ("f_posq", c_float_p)]
+                ("b_self", c_float_p), ("dem_count", c_int_p), ("dem_aux", c_float_p), ("f_posq", c_float_p),
+                ("nbr", c_int_p)]
 
 
 class ParamsT(C.Structure):
@@ -69,7 +70,7 @@ class ParamsT(C.Structure):
         ("shepard_step", C.c_int32)] + [(n, C.c_float) for n in (
             "porosity_min", "porosity_max", "radius_max", "boundary_radius_max", "h_max", "h_uniform")] + [
         ("block_sph", C.c_int32), ("porosity_variant", C.c_int32), ("lanes_sph", C.c_int32),
-        ("pad_params", C.c_int32)]
+        ("nbr_cap", C.c_int32)]
 
 
 class CtxT(C.Structure):

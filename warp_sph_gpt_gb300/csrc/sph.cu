@@ -16,6 +16,15 @@
 //                    (kernel/KERNEL_SPHDEM_interaction.py:97-112): same
 //                    neighbours, same support, one loop.
 //   k_step_sph       Kernel_step_sph (kernel/KERNEL_step.py:6-22).
+//
+// Neighbour lists (one thread per subject): the density pass already decides
+// every fluid-fluid and fluid-wall membership of the step (same support, same
+// exact predicate as the force pass), so it records the member slots in walk
+// order; the force pass then loops over exactly those slots instead of
+// walking its cells again.  A thread walking cells evaluates the force body
+// for ~1 in 5 candidates, and the warp pays for the body on every candidate
+// some lane accepts; from the list every iteration is a member.  Same
+// members, same order, same arithmetic: the forces are bit-identical.
 #include "common.cuh"
 
 namespace sd {
@@ -64,6 +73,8 @@ struct DensArgs {
     float* pres;
     float4* f_rp;    // out: rho, pres, pres/rho^2, 1/rho  (sorted)
     float4* f_posv;  // out: x, y, z, m/rho                 (sorted)
+    int* nbr;        // out: neighbour lists (sphdem_work_t.nbr), or null
+    int cap;
     int n;
     float s2, rq;
     Kern kern;
@@ -79,6 +90,9 @@ __global__ void __launch_bounds__(256) k_density(DensArgs a) {
     const float4 p = a.f_posm[k];
     const int inst = inst_of(a.gs, o);
     float rho_sum = 0.0f, flt_sum = 0.0f;
+    const bool list = LANES == 1 && a.nbr != nullptr;
+    const size_t n = (size_t)a.n;
+    int cf = 0, cb = 0;
     visit_ball<LANES>(a.gs, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
         const float4 q = a.f_posm[j];
         const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
@@ -86,6 +100,10 @@ __global__ void __launch_bounds__(256) k_density(DensArgs a) {
             const float w = kern_w(a.kern, fast_sqrt(r.d2));
             if (RHO) rho_sum += q.w * w;
             if (FLT) flt_sum += a.f_vprev[j] * w;
+            if (list) {
+                if (cf < a.cap) a.nbr[(size_t)cf * n + k] = j;
+                ++cf;
+            }
         }
     });
     if (a.gb.ncl > 0) {
@@ -96,8 +114,16 @@ __global__ void __launch_bounds__(256) k_density(DensArgs a) {
                 const float w = kern_w(a.kern, fast_sqrt(r.d2));
                 if (RHO) rho_sum += q.w * w;
                 if (FLT) flt_sum += a.b_vprev[j] * w;
+                if (list) {
+                    if (cb < a.cap) a.nbr[(size_t)(a.cap + cb) * n + k] = j;
+                    ++cb;
+                }
             }
         });
+    }
+    if (list) {
+        a.nbr[(size_t)(2 * a.cap) * n + k] = cf;
+        a.nbr[(size_t)(2 * a.cap + 1) * n + k] = cb;
     }
     if (RHO) rho_sum = lanes_sum<LANES>(rho_sum);
     if (FLT) flt_sum = lanes_sum<LANES>(flt_sum);
@@ -169,7 +195,9 @@ struct ForceArgs {
     const float4* __restrict__ b_rp;
     float* acc;
     float* pgf;
-    float4* f_pgf;  // out (sorted): pgf x, y, z, rho
+    float4* f_pgf;     // out (sorted): pgf x, y, z, rho
+    const int* nbr;    // neighbour lists of this step's density pass, or null
+    int cap;
     int n;
     float s2, rq;
     Kern kern;
@@ -215,19 +243,42 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
     const float4 rpi = a.f_rp[k];
     const int inst = inst_of(a.gs, o);
     float3 acc = make_float3(0.f, 0.f, 0.f), pgf = make_float3(0.f, 0.f, 0.f);
-    visit_ball<LANES>(a.gs, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
-        const float4 q = a.f_posm[j];
-        const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-        if (r.d2 > kR2Min && r.d2 < a.s2)
-            force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.f_rp[j], a.f_vel, j, acc, pgf);
-    });
-    if (a.gb.ncl > 0) {
-        visit_ball<LANES>(a.gb, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
-            const float4 q = a.b_posm[j];
+    bool walk = true;
+    if (LANES == 1 && a.nbr != nullptr) {
+        // the members recorded by the density pass (all with d2 < s2), in walk order
+        const size_t n = (size_t)a.n;
+        const int cf = a.nbr[(size_t)(2 * a.cap) * n + k], cb = a.nbr[(size_t)(2 * a.cap + 1) * n + k];
+        if (cf <= a.cap && cb <= a.cap) {
+            walk = false;
+            for (int t = 0; t < cf; ++t) {
+                const int j = a.nbr[(size_t)t * n + k];
+                const float4 q = a.f_posm[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 > kR2Min) force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.f_rp[j], a.f_vel, j, acc, pgf);
+            }
+            for (int t = 0; t < cb; ++t) {
+                const int j = a.nbr[(size_t)(a.cap + t) * n + k];
+                const float4 q = a.b_posm[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 > kR2Min) force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.b_rp[j], a.b_vel, j, acc, pgf);
+            }
+        }
+    }
+    if (walk) {
+        visit_ball<LANES>(a.gs, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+            const float4 q = a.f_posm[j];
             const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
             if (r.d2 > kR2Min && r.d2 < a.s2)
-                force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.b_rp[j], a.b_vel, j, acc, pgf);
+                force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.f_rp[j], a.f_vel, j, acc, pgf);
         });
+        if (a.gb.ncl > 0) {
+            visit_ball<LANES>(a.gb, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+                const float4 q = a.b_posm[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 > kR2Min && r.d2 < a.s2)
+                    force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.b_rp[j], a.b_vel, j, acc, pgf);
+            });
+        }
     }
     if (MODE & 1) {
         acc.x = lanes_sum<LANES>(acc.x);
@@ -268,7 +319,7 @@ static float tait_B(float rho0, float c0, float gamma) { return rho0 * c0 * c0 /
 static int launch_block(int b) { return (b == 64 || b == 256) ? b : 128; }
 
 int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
-                float gamma, cudaStream_t st, int block, int lanes) {
+                float gamma, cudaStream_t st, int block, int lanes, int nbr_cap) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     DensArgs a;
@@ -284,6 +335,8 @@ int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rh
     a.pres = c->sph.pres;
     a.f_rp = (float4*)c->work.f_rp;
     a.f_posv = (float4*)c->work.f_posv;
+    a.nbr = (nbr_cap > 0 && lanes != 32) ? c->work.nbr : nullptr;
+    a.cap = nbr_cap;
     a.n = n;
     a.s2 = support * support;
     a.rq = pad_radius(support);
@@ -358,7 +411,7 @@ int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, f
 }
 
 int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st, int block,
-              int lanes) {
+              int lanes, int nbr_cap) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     ForceArgs a;
@@ -374,6 +427,8 @@ int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, 
     a.acc = c->sph.acc;
     a.pgf = c->sph.pgf;
     a.f_pgf = (float4*)c->work.f_pgf;
+    a.nbr = (nbr_cap > 0 && lanes != 32) ? c->work.nbr : nullptr;
+    a.cap = nbr_cap;
     a.n = n;
     a.s2 = support * support;
     a.rq = pad_radius(support);

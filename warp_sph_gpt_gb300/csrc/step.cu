@@ -26,11 +26,11 @@ int gather_fluid(const sphdem_ctx_t* c, cudaStream_t st);
 int gather_wall(const sphdem_ctx_t* c, float support, float h, cudaStream_t st);
 int gather_wall_rho(const sphdem_ctx_t* c, cudaStream_t st);
 int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
-                float gamma, cudaStream_t st, int block = 0, int lanes = 1);
+                float gamma, cudaStream_t st, int block = 0, int lanes = 1, int nbr_cap = 0);
 int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, float rho0, float c0, float gamma,
                      cudaStream_t st, int block = 0, int lanes = 1);
 int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st,
-              int block = 0, int lanes = 1);
+              int block = 0, int lanes = 1, int nbr_cap = 0);
 int run_pres(const float* rho, float* pres, int n, float rho0, float c0, float gamma, cudaStream_t st);
 int run_step_sph(const sphdem_ctx_t* c, float dt, cudaStream_t st);
 int run_contacts(const sphdem_ctx_t* c, float radius_max, float bnd_radius_max, float g, float dt, int which,
@@ -70,6 +70,12 @@ int launch_status(const char* where) {
 
 namespace {
 
+// Neighbour lists between the density and force passes of a step, when the
+// context provides their buffer.
+int nbr_cap(const sphdem_ctx_t* c, const sphdem_params_t* p) {
+    return (c->work.nbr != nullptr && p->nbr_cap > 0) ? p->nbr_cap : 0;
+}
+
 bool shepard_due(const sphdem_params_t* p, int step) {
     return step == 0 || (p->shepard_step > 0 && step % p->shepard_step == 0);  // source/Simulation.py:45
 }
@@ -79,11 +85,13 @@ bool shepard_due(const sphdem_params_t* p, int step) {
 // write_pgf; the acceleration arithmetic is the same either way.
 int sph_part(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool write_pgf, cudaStream_t st) {
     if (shep) TRY(gather_wall_rho(c, st));
-    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
+    const int cap = nbr_cap(c, p);
+    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
+                    cap));
     TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
     sphdem_ctx_t cc = *c;
     if (!write_pgf) cc.sph.pgf = nullptr;
-    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph);
+    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, cap);
 }
 
 int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integrate, cudaStream_t st) {
@@ -645,13 +653,16 @@ int sphdem_profile_step(sphdem_ctx_t* c, const sphdem_params_t* p, int step, int
         if (coupled && (rc = build_grid(&c->grid_dem, c->dem.pos, c->ctl, st))) break;
         mark();
         if (shep && (rc = gather_wall_rho(c, st))) break;
-        if ((rc = run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph))) break;
+        if ((rc = run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph,
+                              p->lanes_sph, nbr_cap(c, p))))
+            break;
         mark();
         if ((rc = run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph))) break;
         mark();
         sphdem_ctx_t cc = *c;
         if (!coupled) cc.sph.pgf = nullptr;
-        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph))) break;
+        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, nbr_cap(c, p))))
+            break;
         mark();
         if (coupled && (rc = run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, st))) break;
         mark();

@@ -9,6 +9,7 @@ host except the explicit status checks and the exact-length CSR views.
 from __future__ import annotations
 
 import ctypes as C
+import math
 import weakref
 
 import torch
@@ -48,7 +49,9 @@ class StepContext:
         self._status_host = torch.zeros(16, dtype=torch.int32, pin_memory=True)
         self._status_event = None
         # launch tuning (results do not depend on it): see autotune.py
-        self.tuning = {"block_sph": 0, "porosity_variant": 0, "lanes_sph": 1}
+        self.tuning = {"block_sph": 0, "porosity_variant": 0, "lanes_sph": 1, "nbr_cap": -1}
+        self._nbr_key = None
+        self._nbr_cap = 0
         self._alloc_work()
         addr = C.addressof(self.ctx)
         weakref.finalize(self, _release, self.lib, addr)
@@ -64,7 +67,32 @@ class StepContext:
             near_list=torch.zeros(ns, **i), b_posm=torch.zeros((nb, 4), **f), b_vel=torch.zeros((nb, 4), **f),
             b_rp=torch.zeros((nb, 4), **f), b_vprev=torch.zeros(nb, **f), b_self=torch.zeros(nb, **f),
             dem_count=torch.zeros(2 * (nd + 1), **i), dem_aux=torch.zeros((nd, 4), **f),
-            f_posq=torch.zeros((ns, 4), **f))
+            f_posq=torch.zeros((ns, 4), **f), nbr=torch.zeros(1, **i))
+
+    NBR_BYTES_MAX = 16 << 30
+
+    def _neighbour_lists(self, solv, request: int = -1) -> int:
+        """Capacity of the density -> force neighbour lists: by default 1.25 x
+        the fluid particles a full support ball holds (from the mean particle
+        volume m / rho0) + 8; ``request`` >= 0 sets it (0 = no lists).  The
+        buffer is allocated once per (support, rho0, request).  Particles with
+        more members walk their cells (same results)."""
+        P = self.sets[0]
+        key = (float(solv.support), float(solv.rho0), int(request))
+        if P.n == 0 or key == self._nbr_key:
+            return self._nbr_cap
+        cap = max(0, int(request))
+        if request < 0:
+            vol = float(P.m.double().mean().item()) / key[1]  # one host sync per key
+            if vol > 0.0:
+                cap = 8 * math.ceil((1.25 * 4.0 / 3.0 * math.pi * key[0] ** 3 / vol + 8.0) / 8.0)
+        if (2 * cap + 2) * P.n * 4 > self.NBR_BYTES_MAX:
+            cap = 0
+        self.work["nbr"] = (torch.zeros((2 * cap + 2) * P.n, dtype=torch.int32, device=self.device) if cap
+                            else torch.zeros(1, dtype=torch.int32, device=self.device))
+        self._nbr_key, self._nbr_cap = key, cap
+        self._sig = None  # pointers changed
+        return cap
 
     def _domain(self):
         """Union bounding box of all particle sets (one host sync, once)."""
@@ -166,6 +194,7 @@ class StepContext:
         p.block_sph = int(self.tuning.get("block_sph", 0))
         p.porosity_variant = int(self.tuning.get("porosity_variant", 0))
         p.lanes_sph = int(self.tuning.get("lanes_sph", 1))
+        p.nbr_cap = self._neighbour_lists(solv, int(self.tuning.get("nbr_cap", -1)))
 
     @property
     def stream(self):
