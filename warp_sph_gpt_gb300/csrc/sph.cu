@@ -250,17 +250,35 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
         const int cf = a.nbr[(size_t)(2 * a.cap) * n + k], cb = a.nbr[(size_t)(2 * a.cap + 1) * n + k];
         if (cf <= a.cap && cb <= a.cap) {
             walk = false;
-            for (int t = 0; t < cf; ++t) {
-                const int j = a.nbr[(size_t)t * n + k];
-                const float4 q = a.f_posm[j];
-                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-                if (r.d2 > kR2Min) force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.f_rp[j], a.f_vel, j, acc, pgf);
+            // four members per round: their slots, then their positions, are
+            // loaded together so the gathers overlap (the loop is latency bound)
+            for (int t = 0; t < cf; t += 4) {
+                int js[4];
+                float4 qs[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) js[u] = t + u < cf ? a.nbr[(size_t)(t + u) * n + k] : k;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) qs[u] = a.f_posm[js[u]];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const D2 r = d2_exact(p.x, p.y, p.z, qs[u].x, qs[u].y, qs[u].z);
+                    if (t + u < cf && r.d2 > kR2Min)
+                        force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, qs[u], a.f_rp[js[u]], a.f_vel, js[u], acc, pgf);
+                }
             }
-            for (int t = 0; t < cb; ++t) {
-                const int j = a.nbr[(size_t)(a.cap + t) * n + k];
-                const float4 q = a.b_posm[j];
-                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-                if (r.d2 > kR2Min) force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, q, a.b_rp[j], a.b_vel, j, acc, pgf);
+            for (int t = 0; t < cb; t += 4) {
+                int js[4];
+                float4 qs[4];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) js[u] = t + u < cb ? a.nbr[(size_t)(a.cap + t + u) * n + k] : 0;
+#pragma unroll
+                for (int u = 0; u < 4; ++u) qs[u] = a.b_posm[js[u]];
+#pragma unroll
+                for (int u = 0; u < 4; ++u) {
+                    const D2 r = d2_exact(p.x, p.y, p.z, qs[u].x, qs[u].y, qs[u].z);
+                    if (t + u < cb && r.d2 > kR2Min)
+                        force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, qs[u], a.b_rp[js[u]], a.b_vel, js[u], acc, pgf);
+                }
             }
         }
     }
