@@ -159,11 +159,27 @@ __device__ __forceinline__ float warp_fluid_sum(const CplArgs& a, int inst, floa
 
 // Solid fraction of a listed particle: the DEM neighbours within 2 h_b, each
 // V_b W(r, h_b) / normaliser (Kernel_prep_sphdem :89-108).  flt is the uniform
-// normaliser; without a uniform h each DEM in reach has its own sum.
+// normaliser: the lanes then take the DEM candidates of each range in turn
+// (lane = offset in the range mod 32) and the terms are summed across the
+// warp.  Without a uniform h each DEM in reach has its own (warp-wide) sum,
+// so the warp walks the candidates together.
 template <bool UNIFORM>
 __device__ __forceinline__ float porosity_solid(const CplArgs& a, const float4& p, int inst, float flt) {
     float solid = 0.0f;
     const Win w = window(a.gd, p.x, p.y, p.z, a.rq);
+    if (UNIFORM) {
+        const int lane = threadIdx.x & 31;
+        for_each_range(a.gd, w, inst, [&](int s, int e) {
+            for (int j = s + lane; j < e; j += 32) {
+                const int b = a.gd.order[j];
+                const float3 pb = ld3(a.D.pos, b);
+                const D2 r = d2_exact(p.x, p.y, p.z, pb.x, pb.y, pb.z);
+                const float4 ab = a.aux[b];
+                if (r.d2 < ab.z) solid += a.D.volume[b] * w_aux(ab, fast_sqrt(r.d2)) / (flt + 1.0e-20f);
+            }
+        });
+        return warp_sum(solid);
+    }
     for_each_range(a.gd, w, inst, [&](int s, int e) {
         for (int j = s; j < e; ++j) {  // warp-uniform loop over DEM candidates
             const int b = a.gd.order[j];
