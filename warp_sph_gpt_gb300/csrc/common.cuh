@@ -160,14 +160,16 @@ __device__ __forceinline__ void column_range_ball(const Geo& g, int cx, int cy, 
 // Warp-cooperative ball enumeration: the 32 lanes trim 32 columns at a time
 // (instead of every lane trimming every column), then f(s, e) is called
 // warp-uniformly for each non-empty range, in column order.
+// With part / parts, the warp takes only every parts-th batch of 32 columns
+// from batch `part` on (the warps of a CTA sharing one ball).
 template <class F>
 __device__ __forceinline__ void warp_ranges_ball(const Geo& g, float px, float py, float pz, float rq, int inst,
-                                                 F&& f) {
+                                                 F&& f, int part = 0, int parts = 1) {
     const int lane = threadIdx.x & 31;
     const Win w = window(g, px, py, pz, rq);
     const int ny = w.y1 - w.y0 + 1;
     const int ncols = (w.x1 - w.x0 + 1) * ny;
-    for (int c0 = 0; c0 < ncols; c0 += 32) {
+    for (int c0 = 32 * part; c0 < ncols; c0 += 32 * parts) {
         int s = 0, e = 0;
         const int c = c0 + lane;
         if (c < ncols) column_range_ball(g, w.x0 + c / ny, w.y0 + c % ny, px, py, pz, rq, inst, s, e);
@@ -177,28 +179,6 @@ __device__ __forceinline__ void warp_ranges_ball(const Geo& g, float px, float p
             mask &= mask - 1;
             f(__shfl_sync(0xffffffffu, s, src), __shfl_sync(0xffffffffu, e, src));
         }
-    }
-}
-
-// Block-cooperative version: the NT threads trim NT columns at a time into
-// shared memory, then f(s, e) is called block-uniformly per non-empty range.
-template <int NT, class F>
-__device__ __forceinline__ void block_ranges_ball(const Geo& g, float px, float py, float pz, float rq, int inst,
-                                                  int* s_sh, int* e_sh, F&& f) {
-    const Win w = window(g, px, py, pz, rq);
-    const int ny = w.y1 - w.y0 + 1;
-    const int ncols = (w.x1 - w.x0 + 1) * ny;
-    for (int c0 = 0; c0 < ncols; c0 += NT) {
-        int s = 0, e = 0;
-        const int c = c0 + (int)threadIdx.x;
-        if (c < ncols) column_range_ball(g, w.x0 + c / ny, w.y0 + c % ny, px, py, pz, rq, inst, s, e);
-        s_sh[threadIdx.x] = s;
-        e_sh[threadIdx.x] = e;
-        __syncthreads();
-        const int m = ncols - c0 < NT ? ncols - c0 : NT;
-        for (int k = 0; k < m; ++k)
-            if (e_sh[k] > s_sh[k]) f(s_sh[k], e_sh[k]);
-        __syncthreads();
     }
 }
 

@@ -9,9 +9,11 @@
 //   k_porosity_near   one warp per listed particle: the fluid normaliser as a
 //                     warp-strided sum over the coupling support, then the solid
 //                     fraction over the DEM neighbours.
-//   k_interaction_dem one CTA per DEM (Kernel_interaction_dem, :118-187): block-
-//                     wide volume-weighted sums of rho, u and -grad p, solid
-//                     fraction, semi-implicit Ergun / Wen-Yu drag, buoyancy.
+//   k_interaction_dem one CTA per DEM (Kernel_interaction_dem, :118-187): its
+//                     warps share the ball's columns; volume-weighted sums of
+//                     rho, u and -grad p reduced over the CTA in fixed order,
+//                     solid fraction, semi-implicit Ergun / Wen-Yu drag,
+//                     buoyancy.
 //   k_react           Kernel_interaction_sph (:190-226) fused with
 //                     Kernel_step_sph (kernel/KERNEL_step.py:6-22).
 // Sums use fixed lane/warp orders, so every result is deterministic.
@@ -443,17 +445,19 @@ constexpr int kIdThreads = 256;
 // Kernel_interaction_dem: one CTA per DEM a.
 __global__ void __launch_bounds__(kIdThreads) k_interaction_dem(CplArgs a) {
     __shared__ float red[kIdThreads / 32][8];
-    __shared__ int s_sh[kIdThreads], e_sh[kIdThreads];
     const int am = blockIdx.x;
     const float3 pa = ld3(a.D.pos, am);
     const float4 aux = a.aux[am];  // 1/h, cw, bound(2h), 2h
     const int inst = inst_of(a.gd, am);
     float s[8] = {0, 0, 0, 0, 0, 0, 0, 0};  // flt, rho_f, vel_f xyz, pgf xyz
     if (a.P.n > 0) {
+        // the warps take turns at 32-column batches of the ball and their
+        // lanes stride through each range (ranges are ~10x longer than a warp
+        // and mostly shorter than the CTA)
         const float t_lo = band_lo(aux.z), t_hi = band_hi(aux.z);
-        block_ranges_ball<kIdThreads>(a.gs, pa.x, pa.y, pa.z, pad_radius(aux.w), inst, s_sh, e_sh,
-                                      [&](int rs, int re) {
-            for (int j = rs + threadIdx.x; j < re; j += blockDim.x) {
+        const int lane = threadIdx.x & 31;
+        warp_ranges_ball(a.gs, pa.x, pa.y, pa.z, pad_radius(aux.w), inst, [&](int rs, int re) {
+            for (int j = rs + lane; j < re; j += 32) {
                 const float4 q = a.f_posv[j];
                 float d2;
                 if (d2_below(pa.x - q.x, pa.y - q.y, pa.z - q.z, t_lo, t_hi, aux.z, d2)) {  // len < 2 h_a, :157-158
@@ -470,7 +474,7 @@ __global__ void __launch_bounds__(kIdThreads) k_interaction_dem(CplArgs a) {
                     s[7] += g.z * Vw;
                 }
             }
-        });
+        }, threadIdx.x >> 5, kIdThreads / 32);
     }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
