@@ -1,6 +1,7 @@
 // grid.cu -- neighbour grid build: counting sort of points by cell.
 //
-// Replaces wp.HashGrid.build (main.py:66,73,85,87).  Steps, all on one stream:
+// Replaces wp.HashGrid.build (main.py:66,73,85,87).  Steps, all on one stream
+// (small grids: all in one CTA, k_build_one):
 //   1. bin      key[i] = cell of point i, count[key]++            (atomics)
 //   2. scan     exclusive prefix sum of the counts -> cell_start   (tiled scan)
 //   3. scatter  order[cell_start[key] + rank] = i                 (atomics)
@@ -111,9 +112,11 @@ __device__ __forceinline__ int warp_bitonic_sort(int v, int lane) {
     return v;
 }
 
-__global__ void k_sort_cells(const int* __restrict__ start, int ncell, int* __restrict__ order) {
-    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+// The 32 cells c0 .. c0 + 31 (this lane: c0 + lane), warp-wide.
+__device__ __forceinline__ void sort_cells_warp(const int* __restrict__ start, int ncell, int* __restrict__ order,
+                                                int c0) {
     const int lane = threadIdx.x & 31;
+    const int c = c0 + lane;
     int s = 0, n = 0;
     if (c < ncell) {
         s = start[c];
@@ -139,6 +142,61 @@ __global__ void k_sort_cells(const int* __restrict__ start, int ncell, int* __re
             order[b + 1] = v;
         }
     }
+}
+
+__global__ void k_sort_cells(const int* __restrict__ start, int ncell, int* __restrict__ order) {
+    sort_cells_warp(start, ncell, order, (blockIdx.x * blockDim.x + threadIdx.x) & ~31);
+}
+
+// The whole build in one CTA, for small grids (at most kOneMaxPoints points
+// and kOneMaxCells cells): the same bin, exclusive scan, scatter and per-cell
+// sort as the multi-kernel path, phase after phase behind __syncthreads, so
+// the cell starts and the order are the same; one launch instead of eight
+// (small systems are bound by launch latency, not by these loops).
+constexpr int kOneThreads = 1024;
+constexpr int kOneMaxPoints = 4096;
+constexpr int kOneMaxCells = 65536;
+
+__global__ void __launch_bounds__(kOneThreads) k_build_one(const float* __restrict__ pos, int n,
+                                                          const int* __restrict__ inst, int lo0, int lo1, int lo2,
+                                                          int d0, int d1, int d2, float inv, int ncl, int ncell,
+                                                          int* __restrict__ key, int* __restrict__ start,
+                                                          int* __restrict__ cursor, int* __restrict__ order,
+                                                          sphdem_ctl_t* ctl) {
+    __shared__ int warp_tot[kOneThreads / 32];
+    const int tid = threadIdx.x;
+    for (int c = tid; c <= ncell; c += kOneThreads) start[c] = 0;
+    for (int c = tid; c < ncell; c += kOneThreads) cursor[c] = 0;
+    __syncthreads();
+    for (int i = tid; i < n; i += kOneThreads) {
+        const float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
+        if (!isfinite(x) || !isfinite(y) || !isfinite(z)) flag(ctl, SPHDEM_FLAG_NONFINITE);
+        const int cx = coord(x, inv, lo0, d0), cy = coord(y, inv, lo1, d1), cz = coord(z, inv, lo2, d2);
+        const int k = (inst ? inst[i] : 0) * ncl + (cx * d1 + cy) * d2 + cz;
+        key[i] = k;
+        atomicAdd(start + k, 1);
+    }
+    __syncthreads();
+    // exclusive scan: each thread a contiguous chunk of cells
+    const int per = (ncell + kOneThreads - 1) / kOneThreads;
+    const int c0 = tid * per, c1 = min(c0 + per, ncell);
+    int sum = 0;
+    for (int c = c0; c < c1; ++c) sum += start[c];
+    int total;
+    int run = block_exclusive_scan(sum, warp_tot, total);
+    for (int c = c0; c < c1; ++c) {
+        const int v = start[c];
+        start[c] = run;
+        run += v;
+    }
+    if (tid == 0) start[ncell] = n;
+    __syncthreads();
+    for (int i = tid; i < n; i += kOneThreads) {
+        const int k = key[i];
+        order[start[k] + atomicAdd(cursor + k, 1)] = i;
+    }
+    __syncthreads();
+    for (int c = tid & ~31; c < ncell; c += kOneThreads) sort_cells_warp(start, ncell, order, c);
 }
 
 __global__ void k_gather_fluid(const int* __restrict__ order, int n, const float* __restrict__ pos,
@@ -210,13 +268,19 @@ int build_grid(sphdem_grid_t* g, const float* pos, sphdem_ctl_t* ctl, cudaStream
         set_error_msg("grid: empty cell box");
         return SPHDEM_ERR_INVALID;
     }
+    const int n = g->n;
+    if (n <= kOneMaxPoints && ncell <= kOneMaxCells) {
+        k_build_one<<<1, kOneThreads, 0, st>>>(pos, n, g->inst, g->lo[0], g->lo[1], g->lo[2], g->dim[0], g->dim[1],
+                                               g->dim[2], g->inv_cell, g->ncell_local, ncell, g->key, g->cell_start,
+                                               g->cursor, g->order, ctl);
+        return launch_status("build_grid");
+    }
     cudaError_t e1 = cudaMemsetAsync(g->cell_start, 0, sizeof(int) * (size_t)(ncell + 1), st);
     cudaError_t e2 = cudaMemsetAsync(g->cursor, 0, sizeof(int) * (size_t)ncell, st);
     if (e1 != cudaSuccess || e2 != cudaSuccess) {
         set_error("grid memset", e1 != cudaSuccess ? e1 : e2);
         return SPHDEM_ERR_CUDA;
     }
-    const int n = g->n;
     if (n > 0)
         k_bin<<<blocks_for(n, 256), 256, 0, st>>>(pos, n, g->inst, g->lo[0], g->lo[1], g->lo[2], g->dim[0],
                                                   g->dim[1], g->dim[2], g->inv_cell, g->ncell_local, g->key,
