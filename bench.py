@@ -511,7 +511,7 @@ def learned_arm(args, rank, world, local_rank):
     prior = S.evaluate(net, ts, val_ids, zero=True)
     t0 = time.perf_counter()
     hist = S.train(net, ts, train_ids, iters=args.train_iters, lr=2e-3, log=log, log_every=500,
-                   edge_weight=args.edge_weight, noise=(args.noise_x, args.noise_v))
+                   edge_weight=args.edge_weight, noise=(args.noise_x, args.noise_v), ema=args.ema)
     torch.cuda.synchronize()
     t_train = time.perf_counter() - t0
     on_policy = []
@@ -528,8 +528,10 @@ def learned_arm(args, rank, world, local_rank):
             for c, s0 in zip(cases, snaps0):
                 c.restore(s0)
             hist += S.train(net, ts, train_ids, iters=args.dagger_iters, lr=1e-3, log=log, log_every=1000,
-                            edge_weight=args.edge_weight, extra=on_policy, seed=rnd + 1)
+                            edge_weight=args.edge_weight, extra=on_policy, seed=rnd + 1, ema=args.ema)
         t_train = time.perf_counter() - t0
+    if args.ema > 0.0:
+        net.use_ema()
     val = S.evaluate(net, ts, val_ids)
     log(f"held-out one-jump loss: prior {prior:.4f} -> trained {val:.4f}")
     del ts, ens
@@ -568,6 +570,15 @@ def learned_arm(args, rank, world, local_rank):
             plain_change.append((plain.P.rho - rho_prev).abs().max().item() / cfg.rho0)
         rho_prev = plain.P.rho.clone()
     plain.restore(plain_final)
+    # the plain method against itself in another FP32 summation order (one
+    # thread per particle instead of one warp): the trajectory's own noise floor
+    alt = Case(config_small(), device=device)
+    alt.tune({"lanes_sph": 1 if default_lanes(alt.P.n) == 32 else 32})
+    alt.run(0, n)
+    alt_err = (alt.P.pos - pos_p).norm(dim=1) / dx
+    plain_reordered = {"pos_max_dx": alt_err.max().item(), "pos_rms_dx": alt_err.pow(2).mean().sqrt().item(),
+                       "order": "same plain step, thread instead of warp per particle"}
+    del alt
     # learned: one plain step + m learned substeps per jump, density judge, plain fallback
     learned = Case(config_small(), device=device)
     learned.tune({"lanes_sph": default_lanes(learned.P.n)})
@@ -599,6 +610,11 @@ def learned_arm(args, rank, world, local_rank):
         t_learned = time.perf_counter() - t0
         torch.cuda.nvtx.range_pop()
     err = (learned.P.pos - pos_p).norm(dim=1) / dx
+    q = torch.quantile(err.float(), torch.tensor([0.99, 0.999], device=device)).tolist()
+    worst = int(err.argmax().item())
+    nd = (pos_p[worst] - dpos_p).norm(dim=1).min().item() / dx if learned.D.n else float("nan")
+    where = {"z_m": pos_p[worst, 2].item(), "speed_mps": vel_p[worst].norm().item(), "nearest_dem_dx": nd,
+             "rho_plain": rho_p[worst].item()}
     derr = (learned.D.pos - dpos_p).norm(dim=1) / dx if learned.D.n else torch.zeros(1, device=device)
     rho_l = _fluid_density(learned)
     rho_dev = ((rho_l - rho_p).abs().max() / cfg.rho0).item()
@@ -634,16 +650,18 @@ def learned_arm(args, rank, world, local_rank):
         "config": {"workload": "learned K-step surrogate vs plain on the config-1 dam break "
                                "(12,500 fluid, 20 DEM, dt=1e-4)", "K": K, "judge_tol": cfg.tol, "judge": cfg.judge,
                    "graph_radius": cfg.radius, "edge_weight": args.edge_weight,
-                   "train_noise": [args.noise_x, args.noise_v], "dagger_rounds": args.dagger_rounds,
+                   "train_noise": [args.noise_x, args.noise_v], "dagger_rounds": args.dagger_rounds, "ema": args.ema,
                    "rollout_steps": n, "fluid": learned.P.n, "dem": learned.D.n,
                    "l2": "state < L2 (resident between steps, as in a run)"},
         "plain": {"value": units * n / t_plain, "ms_per_step": t_plain * 1e3 / n, "clocks": clocks_plain.summary()},
         "speedup_vs_plain": t_plain / t_learned,
         "error_vs_plain": {"pos_max_dx": err.max().item(), "pos_rms_dx": err.pow(2).mean().sqrt().item(),
+                           "pos_p99_dx": q[0], "pos_p999_dx": q[1], "worst_particle": where,
                            "dem_pos_max_dx": derr.max().item(), "rho_max_diff": rho_dev, "rho_rms_diff": rho_rms,
                            "learned_final_density_deviation": ((rho_l - cfg.rho0).abs().max() / cfg.rho0).item(),
                            "plain_final_density_deviation": ((rho_p - cfg.rho0).abs().max() / cfg.rho0).item(),
                            "judge_max_dev_accepted": stats["max_dev_accepted"]},
+        "plain_reordered_vs_plain": plain_reordered,
         "plain_density_deviation": {"max": max(plain_dev), "mean": sum(plain_dev) / len(plain_dev),
                                     "fraction_above_tol": sum(d > cfg.tol for d in plain_dev) / len(plain_dev)},
         "plain_density_change_per_jump": {"max": max(plain_change), "mean": sum(plain_change) / len(plain_change),
@@ -787,6 +805,7 @@ def main():
     ap.add_argument("--train-iters", type=int, default=10000, help="learned: Adam iterations")
     ap.add_argument("--rollout-steps", type=int, default=1000, help="learned: steps of the compared rollouts")
     ap.add_argument("--judge-tol", type=float, default=0.01, help="learned: density judge tolerance / rho0")
+    ap.add_argument("--ema", type=float, default=0.0, help="learned: parameter moving-average decay (0 = off)")
     ap.add_argument("--dagger-rounds", type=int, default=2,
                     help="learned: rounds of on-policy data (states of judged learned rollouts + plain targets)")
     ap.add_argument("--dagger-cases", type=int, default=16, help="learned: training members rolled out per round")

@@ -81,6 +81,7 @@ class Network:
         self.m = torch.zeros_like(self.theta)
         self.v = torch.zeros_like(self.theta)
         self.grad = torch.zeros_like(self.theta)
+        self.ema = None  # exponential moving average of theta (train(..., ema=decay))
         self.step = 0
         self.lib = _lib.load()
         self.pack()
@@ -96,6 +97,18 @@ class Network:
         _lib.check(self.lib.sphdem_mpnn_adam(_p(self.theta), _p(self.grad), _p(self.m), _p(self.v), NPARAM,
                                              lr, beta1, beta2, eps, self.step, self.stream()), "mpnn_adam")
         self.pack()
+
+    def ema_update(self, decay: float) -> None:
+        if self.ema is None:
+            self.ema = self.theta.clone()
+        else:
+            self.ema.lerp_(self.theta, 1.0 - decay)
+
+    def use_ema(self) -> None:
+        """Take the averaged parameters as the network's (and repack)."""
+        if self.ema is not None:
+            self.theta.copy_(self.ema)
+            self.pack()
 
     def state(self) -> dict:
         c = self.cfg
@@ -561,13 +574,16 @@ def _pad_slice(t, start, n):
 
 def train(net: Network, ts: TrainingSet, members, iters: int, lr: float = 1e-3, seed: int = 0, log=None,
           log_every: int = 200, edge_weight: float = 0.0, noise: tuple = (0.0, 0.0), extra=None,
-          extra_fraction: float = 0.5) -> list:
+          extra_fraction: float = 0.5, ema: float = 0.0) -> list:
     """Adam on single-member samples drawn uniformly from the training set.
     edge_weight > 0 adds the edge term (relative displacement errors of
     neighbours, which is what the density judge sees) to the loss; noise =
     (sigma_x [m], sigma_v [m/s]) perturbs the inputs (targets unchanged);
     extra = [(sets, x_t, v_t), ...] samples (collect_on_policy) drawn with
-    probability extra_fraction."""
+    probability extra_fraction.  ema > 0 keeps an exponential moving average
+    of the parameters with that decay (Network.use_ema takes it): each
+    iteration's gradient comes from one member's graph, so the averaged
+    weights are less noisy than the last iterate."""
     rng = np.random.default_rng(seed)
     gen = torch.Generator(device=net.device).manual_seed(seed)
     lib = net.lib
@@ -593,6 +609,8 @@ def train(net: Network, ts: TrainingSet, members, iters: int, lr: float = 1e-3, 
         g.backward(net)
         cos = 0.5 * (1.0 + math.cos(math.pi * it / max(iters, 1)))
         net.adam(lr * (0.05 + 0.95 * cos))
+        if ema > 0.0:
+            net.ema_update(ema)
         if log_every and (it % log_every == 0 or it == iters - 1):
             hist.append((it, L.item()))
             if log:
