@@ -645,6 +645,7 @@ class LearnedRollout:
         self.dev = torch.zeros(1, dtype=torch.float32, device=net.device)
         self.host = torch.zeros(3, dtype=torch.float32).pin_memory()
         self.jump = None
+        self._kernels = {}
         self.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0,
                           jump_kernels=0)
 
@@ -678,16 +679,20 @@ class LearnedRollout:
         ctx, D = self.ctx, c.D
         step, end = first_step, first_step + n_steps
         st = self.g.stream()
+        ctx.set_params(c.solv, c.scales)  # constant over the rollout (the plain fallback sets its own)
         while step < end:
             if end - step < K:
                 c.run(step, end - step)
                 self.stats["plain_steps"] += end - step
                 break
-            ctx.set_params(c.solv, c.scales)
             _lib.check(lib.sphdem_jump(C.byref(ctx.ctx), C.byref(ctx.params), C.byref(self.jump), step, st),
                        "sphdem_jump")
             shep = step == 0 or (c.solv.shepard_step > 0 and step % c.solv.shepard_step == 0)
-            self.stats["jump_kernels"] += max(0, int(lib.sphdem_jump_kernels(C.byref(ctx.ctx), int(shep))))
+            nk = self._kernels.get(shep, 0)  # kernel nodes of this Shepard variant's jump graph
+            if nk <= 0:  # (0 until the graph is captured: the first jumps run eagerly)
+                nk = max(0, int(lib.sphdem_jump_kernels(C.byref(ctx.ctx), int(shep))))
+                self._kernels[shep] = nk
+            self.stats["jump_kernels"] += nk
             D._flip("dem")  # the plain step of the jump swapped both contact CSRs
             D._flip("bnd")
             self.host[0:1].copy_(self.dev, non_blocking=True)
@@ -704,6 +709,7 @@ class LearnedRollout:
                 self.g.ctl[3] = 0
                 self.g._alloc_edges(int(self.g.capacity * 1.5))
                 self.jump = None
+                self._kernels = {}
             elif gflags:
                 raise RuntimeError(f"learned jump raised device status 0x{gflags:x}")
             if self.jump is not None and dev <= cfg.tol:
