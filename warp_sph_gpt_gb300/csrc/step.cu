@@ -100,10 +100,11 @@ int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integ
     return SPHDEM_OK;
 }
 
-// A side stream and two events per device for the concurrent DEM branch.
+// Two side streams and their fork/join events per device: the DEM contact
+// branch and the porosity branch.
 struct Fork {
-    cudaStream_t side = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr;
+    cudaStream_t side = nullptr, side2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr;
 };
 std::mutex g_fork_mu;
 Fork g_fork[64];
@@ -115,8 +116,11 @@ int fork_for_current_device(Fork** out) {
     Fork& f = g_fork[dev];
     if (!f.side) {
         cudaError_t e = cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&f.side2, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.fork2, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join2, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             set_error("fork stream", e);
             return SPHDEM_ERR_CUDA;
@@ -126,10 +130,24 @@ int fork_for_current_device(Fork** out) {
     return SPHDEM_OK;
 }
 
+// Event fork of `side` from `st` (rec on st, side waits).
+int fork_to(cudaStream_t st, cudaStream_t side, cudaEvent_t ev) {
+    cudaError_t e = cudaEventRecord(ev, st);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev, 0);
+    if (e != cudaSuccess) {
+        set_error("fork", e);
+        return SPHDEM_ERR_CUDA;
+    }
+    return SPHDEM_OK;
+}
+
 // The DEM contact rebuild reads only DEM and wall-sphere state, so it runs on
-// a side stream while the fluid density / force / porosity chain runs on the
-// main one (a fork/join of events; inside a graph capture this becomes two
-// parallel branches); the fluid -> DEM exchange waits for both.
+// a side stream while the fluid chain runs on the main one.  The porosity
+// pass needs only positions, the densities' m/rho (f_posv) and the DEM
+// constants, so it forks off after the fluid density and runs beside the wall
+// density and force passes (none of which reads or writes what it does).
+// Fork/join by events; inside a graph capture these are parallel branches.
+// The fluid -> DEM exchange waits for all three.
 int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st) {
     TRY(run_dem_aux(c, st));
     Fork* f = nullptr;
@@ -146,10 +164,23 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
         set_error("join record", e);
         return SPHDEM_ERR_CUDA;
     }
-    TRY(sph_part(c, p, shep, true, st));
+    // sph_part, with the porosity branch forked after the density pass
+    if (shep) TRY(gather_wall_rho(c, st));
+    const int cap = nbr_cap(c, p);
+    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
+                    cap));
+    TRY(fork_to(st, f->side2, f->fork2));
     const float support = 2.0f * p->h_max;  // source/Simulation.py:208
-    TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, st, p->porosity_variant));
-    e = cudaStreamWaitEvent(st, f->join, 0);
+    TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, f->side2, p->porosity_variant));
+    e = cudaEventRecord(f->join2, f->side2);
+    if (e != cudaSuccess) {
+        set_error("join record", e);
+        return SPHDEM_ERR_CUDA;
+    }
+    TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
+    TRY(run_force(c, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, cap));
+    e = cudaStreamWaitEvent(st, f->join2, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, f->join, 0);
     if (e != cudaSuccess) {
         set_error("join", e);
         return SPHDEM_ERR_CUDA;
