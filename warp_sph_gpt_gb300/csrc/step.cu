@@ -104,7 +104,7 @@ int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integ
 // branch and the porosity branch.
 struct Fork {
     cudaStream_t side = nullptr, side2 = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr, ready = nullptr;
 };
 std::mutex g_fork_mu;
 Fork g_fork[64];
@@ -121,6 +121,7 @@ int fork_for_current_device(Fork** out) {
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.fork2, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join2, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.ready, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             set_error("fork stream", e);
             return SPHDEM_ERR_CUDA;
@@ -147,15 +148,17 @@ int fork_to(cudaStream_t st, cudaStream_t side, cudaEvent_t ev) {
 // constants, so it forks off after the fluid density and runs beside the wall
 // density and force passes (none of which reads or writes what it does).
 // Fork/join by events; inside a graph capture these are parallel branches.
-// The fluid -> DEM exchange waits for all three.
-int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st) {
-    TRY(run_dem_aux(c, st));
+// The fluid -> DEM exchange waits for all three.  With build, the step first
+// re-bins its moving grids: the DEM grid on the contact branch, the fluid grid
+// on the main stream, and the porosity branch waits for both.
+int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st, bool build = false) {
     Fork* f = nullptr;
     TRY(fork_for_current_device(&f));
-    cudaError_t e = cudaEventRecord(f->fork, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(f->side, f->fork, 0);
+    TRY(fork_to(st, f->side, f->fork));
+    if (build) TRY(build_grid(&c->grid_dem, c->dem.pos, c->ctl, f->side));
+    cudaError_t e = cudaEventRecord(f->ready, f->side);
     if (e != cudaSuccess) {
-        set_error("fork", e);
+        set_error("ready record", e);
         return SPHDEM_ERR_CUDA;
     }
     TRY(run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, f->side));
@@ -164,11 +167,21 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
         set_error("join record", e);
         return SPHDEM_ERR_CUDA;
     }
+    if (build) {
+        TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
+        TRY(gather_fluid(c, st));
+    }
+    TRY(run_dem_aux(c, st));
     // sph_part, with the porosity branch forked after the density pass
     if (shep) TRY(gather_wall_rho(c, st));
     const int cap = nbr_cap(c, p);
     TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
                     cap));
+    e = cudaStreamWaitEvent(st, f->ready, 0);  // the porosity pass reads the DEM grid
+    if (e != cudaSuccess) {
+        set_error("ready wait", e);
+        return SPHDEM_ERR_CUDA;
+    }
     TRY(fork_to(st, f->side2, f->fork2));
     const float support = 2.0f * p->h_max;  // source/Simulation.py:208
     TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, f->side2, p->porosity_variant));
@@ -244,12 +257,9 @@ void drop_entry(GraphEntry& e) {
 }
 
 int loop_body(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, int coupled, cudaStream_t st) {
+    if (coupled) return coupled_onestep(c, p, shep, st, true);
     TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
     TRY(gather_fluid(c, st));
-    if (coupled) {
-        TRY(build_grid(&c->grid_dem, c->dem.pos, c->ctl, st));
-        return coupled_onestep(c, p, shep, st);
-    }
     return sph_onestep(c, p, shep, true, st);
 }
 
