@@ -148,7 +148,8 @@ int fork_to(cudaStream_t st, cudaStream_t side, cudaEvent_t ev) {
 // constants, so it forks off after the fluid density and runs beside the wall
 // density and force passes (none of which reads or writes what it does).
 // Fork/join by events; inside a graph capture these are parallel branches.
-// The fluid -> DEM exchange waits for all three.  With build, the step first
+// The fluid -> DEM exchange waits for the contacts and the force pass, the
+// reaction on the fluid for the porosity branch too.  With build, the step first
 // re-bins its moving grids: the DEM grid on the contact branch, the fluid grid
 // on the main stream, and the porosity branch waits for both.
 int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st, bool build = false) {
@@ -192,13 +193,19 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
     }
     TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
     TRY(run_force(c, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, cap));
-    e = cudaStreamWaitEvent(st, f->join2, 0);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(st, f->join, 0);
+    // the exchange adds to the contact forces and reads -grad p, not the fluid
+    // porosity, so it runs beside the porosity branch; the reaction needs both
+    e = cudaStreamWaitEvent(st, f->join, 0);
     if (e != cudaSuccess) {
         set_error("join", e);
         return SPHDEM_ERR_CUDA;
     }
     TRY(run_interaction_dem(c, p->mu, p->porosity_min, p->porosity_max, p->dt, st));
+    e = cudaStreamWaitEvent(st, f->join2, 0);
+    if (e != cudaSuccess) {
+        set_error("join", e);
+        return SPHDEM_ERR_CUDA;
+    }
     TRY(run_react(c, support, p->dt, true, st));
     return run_step_dem(c, p->dt, st);
 }
