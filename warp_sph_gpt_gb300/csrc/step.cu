@@ -103,8 +103,9 @@ int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integ
 // Two side streams and their fork/join events per device: the DEM contact
 // branch and the porosity branch.
 struct Fork {
-    cudaStream_t side = nullptr, side2 = nullptr;
-    cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr, ready = nullptr;
+    cudaStream_t side = nullptr, side2 = nullptr, side3 = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr, fork2 = nullptr, join2 = nullptr, ready = nullptr, wall = nullptr,
+                dens = nullptr;
 };
 std::mutex g_fork_mu;
 Fork g_fork[64];
@@ -117,11 +118,14 @@ int fork_for_current_device(Fork** out) {
     if (!f.side) {
         cudaError_t e = cudaStreamCreateWithFlags(&f.side, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&f.side2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&f.side3, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.fork, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.fork2, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.join2, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.ready, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.wall, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&f.dens, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             set_error("fork stream", e);
             return SPHDEM_ERR_CUDA;
@@ -131,81 +135,68 @@ int fork_for_current_device(Fork** out) {
     return SPHDEM_OK;
 }
 
-// Event fork of `side` from `st` (rec on st, side waits).
-int fork_to(cudaStream_t st, cudaStream_t side, cudaEvent_t ev) {
-    cudaError_t e = cudaEventRecord(ev, st);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(side, ev, 0);
-    if (e != cudaSuccess) {
-        set_error("fork", e);
-        return SPHDEM_ERR_CUDA;
-    }
-    return SPHDEM_OK;
-}
-
-// The DEM contact rebuild reads only DEM and wall-sphere state, so it runs on
-// a side stream while the fluid chain runs on the main one.  The porosity
-// pass needs only positions, the densities' m/rho (f_posv) and the DEM
-// constants, so it forks off after the fluid density and runs beside the wall
-// density and force passes (none of which reads or writes what it does).
-// Fork/join by events; inside a graph capture these are parallel branches.
-// The fluid -> DEM exchange waits for the contacts and the force pass, the
-// reaction on the fluid for the porosity branch too.  With build, the step first
-// re-bins its moving grids: the DEM grid on the contact branch, the fluid grid
-// on the main stream, and the porosity branch waits for both.
+// Three branches per step, forked and joined by events (inside a graph
+// capture they become parallel branches of the graph):
+//   contact branch: [DEM grid re-bin] -> DEM-DEM / DEM-wall contacts; it reads
+//                   only DEM and wall-sphere state.
+//   main:           [fluid grid re-bin + gather] -> DEM constants -> [wall
+//                   m/rho for the Shepard filter] -> fluid density -> force
+//                   (after the wall density) -> fluid -> DEM exchange (after
+//                   the contacts: it adds to their forces; it reads -grad p,
+//                   not the fluid porosity) -> reaction on the fluid and
+//                   integrators (after the porosity branch).
+//   wall branch:    wall density (it reads only positions and masses).
+//   porosity branch: porosity, once the fluid density (m/rho) and the DEM
+//                   grid are ready.
+// build: the step first re-bins its moving grids (the loop body); the
+// single-call API has built them already.
 int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st, bool build = false) {
     Fork* f = nullptr;
     TRY(fork_for_current_device(&f));
-    TRY(fork_to(st, f->side, f->fork));
+    auto rec = [&](cudaEvent_t ev, cudaStream_t s) {
+        const cudaError_t e = cudaEventRecord(ev, s);
+        if (e != cudaSuccess) set_error("event record", e);
+        return e == cudaSuccess ? SPHDEM_OK : SPHDEM_ERR_CUDA;
+    };
+    auto wait = [&](cudaStream_t s, cudaEvent_t ev) {
+        const cudaError_t e = cudaStreamWaitEvent(s, ev, 0);
+        if (e != cudaSuccess) set_error("event wait", e);
+        return e == cudaSuccess ? SPHDEM_OK : SPHDEM_ERR_CUDA;
+    };
+    // contact branch
+    TRY(rec(f->fork, st));
+    TRY(wait(f->side, f->fork));
     if (build) TRY(build_grid(&c->grid_dem, c->dem.pos, c->ctl, f->side));
-    cudaError_t e = cudaEventRecord(f->ready, f->side);
-    if (e != cudaSuccess) {
-        set_error("ready record", e);
-        return SPHDEM_ERR_CUDA;
-    }
+    TRY(rec(f->ready, f->side));
     TRY(run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, f->side));
-    e = cudaEventRecord(f->join, f->side);
-    if (e != cudaSuccess) {
-        set_error("join record", e);
-        return SPHDEM_ERR_CUDA;
-    }
+    TRY(rec(f->join, f->side));
+    // main, up to the fork of the porosity branch
     if (build) {
         TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
         TRY(gather_fluid(c, st));
     }
     TRY(run_dem_aux(c, st));
-    // sph_part, with the porosity branch forked after the density pass
     if (shep) TRY(gather_wall_rho(c, st));
+    TRY(rec(f->fork2, st));
+    TRY(wait(f->side3, f->fork2));
+    TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, f->side3, p->block_sph, p->lanes_sph));
+    TRY(rec(f->wall, f->side3));
     const int cap = nbr_cap(c, p);
     TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
                     cap));
-    e = cudaStreamWaitEvent(st, f->ready, 0);  // the porosity pass reads the DEM grid
-    if (e != cudaSuccess) {
-        set_error("ready wait", e);
-        return SPHDEM_ERR_CUDA;
-    }
-    TRY(fork_to(st, f->side2, f->fork2));
+    TRY(rec(f->dens, st));
+    // porosity branch
+    TRY(wait(f->side2, f->dens));
+    TRY(wait(f->side2, f->ready));
     const float support = 2.0f * p->h_max;  // source/Simulation.py:208
     TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, f->side2, p->porosity_variant));
-    e = cudaEventRecord(f->join2, f->side2);
-    if (e != cudaSuccess) {
-        set_error("join record", e);
-        return SPHDEM_ERR_CUDA;
-    }
-    TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
+    TRY(rec(f->join2, f->side2));
+    // main, continued
+    TRY(wait(st, f->wall));
     TRY(run_force(c, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, cap));
-    // the exchange adds to the contact forces and reads -grad p, not the fluid
-    // porosity, so it runs beside the porosity branch; the reaction needs both
-    e = cudaStreamWaitEvent(st, f->join, 0);
-    if (e != cudaSuccess) {
-        set_error("join", e);
-        return SPHDEM_ERR_CUDA;
-    }
+    TRY(wait(st, f->join));
     TRY(run_interaction_dem(c, p->mu, p->porosity_min, p->porosity_max, p->dt, st));
-    e = cudaStreamWaitEvent(st, f->join2, 0);
-    if (e != cudaSuccess) {
-        set_error("join", e);
-        return SPHDEM_ERR_CUDA;
-    }
+    TRY(wait(st, f->join2));
     TRY(run_react(c, support, p->dt, true, st));
     return run_step_dem(c, p->dt, st);
 }
