@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPHDEM_ABI_VERSION 8
+#define SPHDEM_ABI_VERSION 9
 
 /* ---- return codes ---------------------------------------------------- */
 #define SPHDEM_OK                0

@@ -93,6 +93,11 @@ typedef struct sphdem_mpnn_net {
     uint16_t* h3;             /* [n_recv,128]                                 */
     float* out;               /* [n_recv,16] FP32                             */
     int32_t* status;          /* device word, OR of SPHDEM_FLAG_* bits        */
+    /* optional (inference): the node layers then run on the receivers and on
+     * the non-receiver nodes that send an edge of the current graph only --
+     * the others' latent rows are never read (NULL: every node) */
+    int32_t* active;          /* [n_nodes] scratch flags                      */
+    int32_t* active_list;     /* [1 + n_nodes - n_recv]: count, then nodes    */
 } sphdem_mpnn_net_t;
 
 /* Backward workspace. */
@@ -195,11 +200,16 @@ typedef struct sphdem_jump {
     int32_t pad_jump;
 } sphdem_jump_t;
 
-int sphdem_jump(sphdem_ctx_t* ctx, const sphdem_params_t* p, const sphdem_jump_t* j, int step,
+/* flags bit 0 (SPHDEM_JUMP_GRID_FRESH): the fluid grid is current -- the last
+ * call on this context was a jump the caller accepted and nothing has moved
+ * the fluid since (its judge re-binned the fluid at these positions) -- so
+ * the plain step skips that re-bin (same grid, same results). */
+#define SPHDEM_JUMP_GRID_FRESH 1
+int sphdem_jump(sphdem_ctx_t* ctx, const sphdem_params_t* p, const sphdem_jump_t* j, int step, int32_t flags,
                 sphdem_stream_t stream);
 
-/* Kernel nodes of the jump's captured graph (variant 1: Shepard step), or -1
- * if that variant has not been captured yet. */
+/* Kernel nodes of the jump's captured graph (variant bit 0: Shepard step, bit
+ * 1: SPHDEM_JUMP_GRID_FRESH), or -1 if that variant has not been captured. */
 int sphdem_jump_kernels(sphdem_ctx_t* ctx, int variant);
 
 /* Restore positions, velocities and fluid density saved by the last jump. */

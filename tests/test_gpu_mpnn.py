@@ -222,3 +222,37 @@ def test_edge_loss_matches_its_formula():
     m = snd < nr
     np.add.at(gref[:, :3], snd[m], -2 * lam / E * diff[m])
     np.testing.assert_allclose(grad - base_grad, gref, rtol=1e-4, atol=1e-7)
+
+
+def test_inference_node_layers_run_on_receivers_and_senders():
+    """The inference pass lists the non-receiver nodes that send an edge
+    (each once) and runs the node layers on the receivers and those only; the
+    output equals the pass over every node (up to the order of the FP32
+    atomics at run boundaries)."""
+    import ctypes as C
+
+    from warp_sph_gpt_gb300.surrogate import Network
+
+    g, cfg, d = _synthetic(5, n=1400, n_recv=500, radius=0.04)
+    net = Network(cfg, "cuda", seed=3)
+    th = net.theta.clone()
+    th[O.N3_W:O.N3_W + 6 * 128] *= 30.0
+    net.theta.copy_(th)
+    net.pack()
+    a = g.forward(net, store_pre=False).clone()
+    torch.cuda.synchronize()
+    nr = d["n_recv"]
+    off = g.buf["offset"][: nr + 1].cpu().numpy()
+    snd = g.buf["sender"][: off[-1]].cpu().numpy()
+    static = np.unique(snd[snd >= nr])
+    lst = g.buf["active_list"].cpu().numpy()
+    assert 0 < lst[0] == len(static) < d["n"] - nr  # some non-receivers send, not all
+    assert np.array_equal(np.sort(lst[1:1 + lst[0]]), static)
+    full = g._net(net)
+    full.active = None
+    full.active_list = None
+    g.lib.sphdem_mpnn_forward(C.byref(full), 0, g.stream())
+    b = g.buf["out"][:nr].clone()
+    torch.cuda.synchronize()
+    err = (a - b).abs().max().item() / max(a.abs().max().item(), 1e-30)
+    assert err <= 1e-3, err

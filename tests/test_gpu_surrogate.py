@@ -12,6 +12,8 @@
 * A rollout of the config-1 dam break with the plain-step fallback keeps its
   accounting (every jump accepted or undone), stays finite, and never accepts
   a jump whose density moved by more than the judge's tolerance.
+* A jump after an accepted one reuses the fluid grid its judge built: that
+  grid is exactly the re-bin of the current positions.
 """
 import numpy as np
 import pytest
@@ -80,3 +82,34 @@ def test_rollout_with_fallback_respects_the_judge(trained):
     assert stats["learned_steps"] == trained["cfg"].substeps * (stats["jumps"] - stats["fallbacks"])
     assert torch.isfinite(case.P.pos).all() and torch.isfinite(case.D.pos).all()
     assert int(ro.g.status()) == 0
+
+
+def test_jump_after_an_accepted_one_reuses_a_current_grid(trained):
+    """After an accepted jump the fluid grid (cell starts and slot order) is
+    exactly the one a re-bin of the current positions builds, so the next jump
+    may skip that re-bin.  (Two whole rollouts are not compared bit for bit:
+    the edge pass combines partial receiver sums across CTAs with atomics.)"""
+    import ctypes as C
+
+    from warp_sph_gpt_gb300 import _lib
+    from warp_sph_gpt_gb300.batch import Case
+    from warp_sph_gpt_gb300.engine import KIND_SPH
+    from warp_sph_gpt_gb300.generate import config_small
+    from warp_sph_gpt_gb300.surrogate import LearnedRollout
+
+    case = Case(config_small())
+    ro = LearnedRollout(case, trained["net"])
+    step = 0
+    while step < 200:
+        ro.run(step, 10)
+        step += 10
+        if ro.last_accepted and step >= 30:
+            break
+    assert ro.last_accepted and ro.stats["jumps"] - ro.stats["fallbacks"] >= 2
+    torch.cuda.synchronize()
+    b = case.grids[0].buffers
+    order, start = b["order"].clone(), b["cell_start"].clone()
+    ctx = ro.ctx
+    _lib.check(ctx.lib.sphdem_grid_build(C.byref(ctx.ctx), KIND_SPH, C.byref(ctx.params), ctx.stream), "grid")
+    torch.cuda.synchronize()
+    assert torch.equal(order, b["order"]) and torch.equal(start, b["cell_start"])

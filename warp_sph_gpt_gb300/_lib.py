@@ -97,7 +97,8 @@ class MpnnNetT(C.Structure):
                 + [("node_pos4", c_float_p), ("node_vel4", c_float_p), ("x", c_u16_p), ("offset", c_int_p),
                    ("sender", c_int_p), ("receiver", c_int_p), ("theta", c_float_p), ("packed", c_u16_p),
                    ("z0", c_float_p), ("h0", c_u16_p), ("agg", c_float_p), ("h1", c_u16_p), ("z2", c_float_p),
-                   ("h2", c_u16_p), ("h3", c_u16_p), ("out", c_float_p), ("status", c_int_p)])
+                   ("h2", c_u16_p), ("h3", c_u16_p), ("out", c_float_p), ("status", c_int_p),
+                   ("active", c_int_p), ("active_list", c_int_p)])
 
 
 class MpnnGradT(C.Structure):
@@ -120,7 +121,7 @@ FLAG_CSR_DEM_OVERFLOW = 0x1
 FLAG_CSR_BND_OVERFLOW = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_TIMEOUT = 0x10
-ABI_VERSION = 8
+ABI_VERSION = 9
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
 REL = dict(SPH_SPH_SUPPORT=0, SPH_BND_SUPPORT=1, BND_SPH_SUPPORT=2, BND_BND_SUPPORT=3, SPH_SPH_FORCE=4,
@@ -181,7 +182,7 @@ _SIGNATURES = {
                            C.c_int),
     "sphdem_mpnn_gemm": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                           C.c_void_p], C.c_int),
-    "sphdem_jump": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "sphdem_jump": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int32, C.c_void_p], C.c_int),
     "sphdem_jump_undo": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_jump_kernels": ([C.c_void_p, C.c_int], C.c_int),
     "sphdem_mpnn_wgrad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,

@@ -155,12 +155,14 @@ __global__ void k_pack(const float* __restrict__ theta, uint16_t* __restrict__ p
 // ---------------------------------------------------------------------------
 // add (optional, K = 128): rows r < n_add of the A operand are A[r] + add[r]
 // (the residual h + s * sum_j f_ij (.) h_j, formed while staging the tile).
+// list (optional): the layer runs on rows 0 .. n_direct - 1 and on the list[0]
+// rows list[1 ..] (in any order: rows are independent); M bounds both.
 template <int K, int N, int EPI, bool IMG>
 __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int M, const float* __restrict__ add,
                                              int n_add, const uint16_t* __restrict__ B,
                                              const float* __restrict__ bias, float* __restrict__ out_f32,
                                              uint16_t* __restrict__ out_bf, float* __restrict__ z_out,
-                                             int32_t* status) {
+                                             int32_t* status, const int* __restrict__ list, int n_direct) {
     constexpr uint32_t kB = N * K * 2, kA = kT * K * 2;
     constexpr uint32_t kCols = N < 32 ? 32 : N;
     extern __shared__ __align__(1024) uint8_t sm[];
@@ -190,8 +192,10 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
     }
     __syncthreads();
     constexpr uint32_t idesc = umma::idesc_bf16(128, N);
-    for (int tile = blockIdx.x; !failed && tile * kT < M; tile += gridDim.x) {
-        const int row = tile * kT + tid;
+    const int Mv = list ? min(M, n_direct + __ldg(list)) : M;  // rows of this launch
+    for (int tile = blockIdx.x; !failed && tile * kT < Mv; tile += gridDim.x) {
+        int row = tile * kT + tid;
+        if (list && row >= n_direct) row = row < Mv ? __ldg(list + 1 + (row - n_direct)) : M;  // M: no row
         const bool plus = add != nullptr && row < n_add;
 #pragma unroll
         for (int q = 0; q < K / 8; ++q) {
@@ -1153,14 +1157,16 @@ int smem_opt_in(Kern k, uint32_t bytes) {
 
 template <int K, int N, int EPI, bool IMG>
 int rows(const uint16_t* A, int M, const uint16_t* B, const float* bias, float* out_f32, uint16_t* out_bf,
-         float* z_out, int32_t* status, cudaStream_t st, const float* add = nullptr, int n_add = 0) {
+         float* z_out, int32_t* status, cudaStream_t st, const float* add = nullptr, int n_add = 0,
+         const int* list = nullptr, int n_direct = 0) {
     if (M <= 0) return SPHDEM_OK;
     constexpr uint32_t bytes = N * K * 2 + kT * K * 2 + 4 * (N < 2 ? 2 : N) + 16 + 16;
     int rc = smem_opt_in(k_rows<K, N, EPI, IMG>, bytes);
     if (rc) return rc;
     const int tiles = (M + kT - 1) / kT;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-    k_rows<K, N, EPI, IMG><<<grid, kT, bytes, st>>>(A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status);
+    k_rows<K, N, EPI, IMG><<<grid, kT, bytes, st>>>(A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status, list,
+                                                    n_direct);
     return launch_status("mpnn rows");
 }
 
@@ -1298,6 +1304,22 @@ extern "C" int sphdem_mpnn_graph(sphdem_grid_t* grid, const float* node_pos3, co
     return launch_status("mpnn_graph");
 }
 
+namespace sd {
+namespace {
+// Non-receiver senders of the current graph, each listed once: list[0] is
+// their count, list[1 ..] the nodes (order immaterial: node rows are
+// independent).  Edge count from the CSR offsets.
+__global__ void k_mark_senders(const int* __restrict__ offset, const int* __restrict__ sender, int n_recv,
+                               int* __restrict__ active, int* __restrict__ list) {
+    const int E = __ldg(offset + n_recv);
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
+        const int s = __ldg(sender + e);
+        if (s >= n_recv && atomicExch(active + s, 1) == 0) list[1 + atomicAdd(list, 1)] = s;
+    }
+}
+}  // namespace
+}  // namespace sd
+
 extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sphdem_stream_t stream) {
     if (!net_ok(n) || (store_pre && (!n->z0 || !n->z2))) {
         set_error_msg("mpnn_forward: invalid network state");
@@ -1305,8 +1327,20 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
     }
     cudaStream_t st = as_stream(stream);
     const int nn = n->n_nodes, nr = n->n_recv;
+    // inference: node layers on the receivers and the other nodes that send
+    const int* list = nullptr;
+    if (!store_pre && n->active && n->active_list && nn > nr) {
+        cudaError_t e = cudaMemsetAsync(n->active, 0, sizeof(int) * (size_t)nn, st);
+        if (e == cudaSuccess) e = cudaMemsetAsync(n->active_list, 0, sizeof(int), st);
+        if (e != cudaSuccess) {
+            set_error("mpnn_forward", e);
+            return SPHDEM_ERR_CUDA;
+        }
+        k_mark_senders<<<2 * sm_count(), 256, 0, st>>>(n->offset, n->sender, nr, n->active, n->active_list);
+        list = n->active_list;
+    }
     int rc = rows<16, 128, EPI_SILU, true>(n->x, nn, n->packed + P_N1, n->theta + SPHDEM_MPNN_N1_B, nullptr, n->h0,
-                                           store_pre ? n->z0 : nullptr, n->status, st);
+                                           store_pre ? n->z0 : nullptr, n->status, st, nullptr, 0, list, nr);
     if (rc) return rc;
     EdgeArgs a = edge_args(n);
     const int eg = edge_grid(n, 1);
@@ -1326,7 +1360,7 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
                                                     nullptr, n->h2, n->z2, n->status, st);
             } else {  // h1 = h0 + agg formed while staging
                 rc = rows<128, 128, EPI_SILU, true>(n->h0, nn, n->packed + P_N2, n->theta + SPHDEM_MPNN_N2_B,
-                                                    nullptr, n->h2, nullptr, n->status, st, n->agg, nr);
+                                                    nullptr, n->h2, nullptr, n->status, st, n->agg, nr, list, nr);
             }
             if (rc) return rc;
         } else if (store_pre) {

@@ -148,9 +148,10 @@ int fork_for_current_device(Fork** out) {
 //   wall branch:    wall density (it reads only positions and masses).
 //   porosity branch: porosity, once the fluid density (m/rho) and the DEM
 //                   grid are ready.
-// build: the step first re-bins its moving grids (the loop body); the
-// single-call API has built them already.
-int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st, bool build = false) {
+// build: the step first re-bins its moving grids (the loop body) -- the
+// fluid grid only if !fluid_fresh; the single-call API has built them already.
+int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st, bool build = false,
+                    bool fluid_fresh = false) {
     Fork* f = nullptr;
     TRY(fork_for_current_device(&f));
     auto rec = [&](cudaEvent_t ev, cudaStream_t s) {
@@ -172,7 +173,7 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
     TRY(rec(f->join, f->side));
     // main, up to the fork of the porosity branch
     if (build) {
-        TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
+        if (!fluid_fresh) TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
         TRY(gather_fluid(c, st));
     }
     TRY(run_dem_aux(c, st));
@@ -553,8 +554,9 @@ int jump_keep(sphdem_ctx_t* c, const sphdem_jump_t* j, bool restore, cudaStream_
     return SPHDEM_OK;
 }
 
-int jump_body(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, bool shep, cudaStream_t st) {
-    TRY(loop_body(c, p, shep, 1, st));
+int jump_body(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, bool shep, bool fresh,
+              cudaStream_t st) {
+    TRY(coupled_onestep(c, p, shep, st, true, fresh));
     TRY(jump_keep(c, j, false, st));
     TRY(sphdem_mpnn_nodes(&j->nodes, st));
     sphdem_grid_t g = j->node_grid;
@@ -581,15 +583,16 @@ struct JumpEntry {
     sphdem_params_t params;
     sphdem_jump_t jump;
     cudaStream_t cap = nullptr;
-    cudaGraphExec_t exec[2] = {nullptr, nullptr};
-    bool warm[2] = {false, false};
-    int kernels[2] = {0, 0};
+    cudaGraphExec_t exec[4] = {nullptr, nullptr, nullptr, nullptr};  // [Shepard + 2 fresh]
+    bool warm[4] = {false, false, false, false};
+    int kernels[4] = {0, 0, 0, 0};
 };
 std::map<const sphdem_ctx_t*, JumpEntry> g_jumps;
 
 }  // namespace
 
-int sphdem_jump(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, int step, sphdem_stream_t stream) {
+int sphdem_jump(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, int step, int32_t flags,
+                sphdem_stream_t stream) {
     if (!valid_ctx(c) || !p || !j || !j->keep || !j->dev || !j->graph_ctl || !j->scan_scratch || j->substeps < 1 ||
         c->dem.n < 0) {
         set_error_msg("jump: invalid arguments");
@@ -606,15 +609,16 @@ int sphdem_jump(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* 
                 cudaGraphExecDestroy(x);
                 x = nullptr;
             }
-        e.warm[0] = e.warm[1] = false;
+        for (auto& w : e.warm) w = false;
         e.snap = *c;
         e.params = *p;
         e.jump = *j;
     }
-    const int v = shep ? 1 : 0;
+    const bool fresh = (flags & SPHDEM_JUMP_GRID_FRESH) != 0;
+    const int v = (shep ? 1 : 0) + (fresh ? 2 : 0);
     if (!e.warm[v]) {  // first use runs eagerly (one-time kernel attribute set-up), later ones replay
         e.warm[v] = true;
-        return jump_body(c, p, j, shep, st);
+        return jump_body(c, p, j, shep, fresh, st);
     }
     if (!e.cap) {
         cudaError_t err = cudaStreamCreateWithFlags(&e.cap, cudaStreamNonBlocking);
@@ -629,7 +633,7 @@ int sphdem_jump(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* 
             set_error("jump capture begin", err);
             return SPHDEM_ERR_CUDA;
         }
-        int rc = jump_body(c, p, j, shep, e.cap);
+        int rc = jump_body(c, p, j, shep, fresh, e.cap);
         cudaGraph_t graph = nullptr;
         err = cudaStreamEndCapture(e.cap, &graph);
         if (rc) {
@@ -659,8 +663,8 @@ int sphdem_jump(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* 
 int sphdem_jump_kernels(sphdem_ctx_t* c, int variant) {
     std::lock_guard<std::mutex> lock(g_graph_mu);
     auto it = g_jumps.find(c);
-    if (it == g_jumps.end() || !it->second.exec[variant ? 1 : 0]) return -1;
-    return it->second.kernels[variant ? 1 : 0];
+    if (it == g_jumps.end() || variant < 0 || variant > 3 || !it->second.exec[variant]) return -1;
+    return it->second.kernels[variant];
 }
 
 int sphdem_jump_undo(sphdem_ctx_t* c, const sphdem_jump_t* j, sphdem_stream_t stream) {

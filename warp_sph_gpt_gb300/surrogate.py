@@ -188,7 +188,8 @@ class Graph:
                             node_vel4=torch.zeros(n, 4, **f32), x=torch.zeros(n, 16, **i16),
                             z0=torch.zeros(n, HIDDEN, **f32), h0=torch.zeros(n, HIDDEN, **i16),
                             h1=torch.zeros(n, HIDDEN, **i16), z2=torch.zeros(n, HIDDEN, **f32),
-                            h2=torch.zeros(n, HIDDEN, **i16))
+                            h2=torch.zeros(n, HIDDEN, **i16), active=torch.zeros(n, dtype=torch.int32, device=dev),
+                            active_list=torch.zeros(n + 1, dtype=torch.int32, device=dev))
             self.gbuf = {}
         if n_recv > self.buf.get("_recv", 0) or "offset" not in self.buf:
             n = int(max(n_recv, 1) * 1.1) + 16
@@ -295,6 +296,7 @@ class Graph:
         n.z0, n.h0, n.agg, n.h1 = _lib.fptr(b["z0"]), u16(b["h0"]), _lib.fptr(b["agg"]), u16(b["h1"])
         n.z2, n.h2, n.h3, n.out = _lib.fptr(b["z2"]), u16(b["h2"]), u16(b["h3"]), _lib.fptr(b["out"])
         n.status = C.cast(self.ctl.data_ptr() + 12, _lib.c_int_p)
+        n.active, n.active_list = _lib.iptr(b["active"]), _lib.iptr(b["active_list"])
         return n
 
     def forward(self, net: Network, store_pre: bool = False) -> torch.Tensor:
@@ -631,10 +633,11 @@ class LearnedRollout:
     above ``tol`` (or on a graph-capacity overflow), undoes the jump and runs
     the m steps with the plain method."""
 
-    def __init__(self, case, net: Network):
+    def __init__(self, case, net: Network, reuse_grid: bool = True):
         from .engine import context_for
 
         self.case = case
+        self.reuse_grid = reuse_grid  # after an accepted jump, its judge's fluid grid serves the next
         self.net = net
         self.cfg = net.cfg
         self.lib = net.lib
@@ -646,6 +649,7 @@ class LearnedRollout:
         self.host = torch.zeros(3, dtype=torch.float32).pin_memory()
         self.jump = None
         self._kernels = {}
+        self.last_accepted = False  # the last jump of the last run() was accepted
         self.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0,
                           jump_kernels=0)
 
@@ -680,18 +684,21 @@ class LearnedRollout:
         step, end = first_step, first_step + n_steps
         st = self.g.stream()
         ctx.set_params(c.solv, c.scales)  # constant over the rollout (the plain fallback sets its own)
+        fresh = 0  # SPHDEM_JUMP_GRID_FRESH: the last call here was an accepted jump
         while step < end:
             if end - step < K:
                 c.run(step, end - step)
                 self.stats["plain_steps"] += end - step
+                self.last_accepted = False
                 break
-            _lib.check(lib.sphdem_jump(C.byref(ctx.ctx), C.byref(ctx.params), C.byref(self.jump), step, st),
+            _lib.check(lib.sphdem_jump(C.byref(ctx.ctx), C.byref(ctx.params), C.byref(self.jump), step, fresh, st),
                        "sphdem_jump")
             shep = step == 0 or (c.solv.shepard_step > 0 and step % c.solv.shepard_step == 0)
-            nk = self._kernels.get(shep, 0)  # kernel nodes of this Shepard variant's jump graph
+            variant = int(shep) + 2 * fresh
+            nk = self._kernels.get(variant, 0)  # kernel nodes of this variant's jump graph
             if nk <= 0:  # (0 until the graph is captured: the first jumps run eagerly)
-                nk = max(0, int(lib.sphdem_jump_kernels(C.byref(ctx.ctx), int(shep))))
-                self._kernels[shep] = nk
+                nk = max(0, int(lib.sphdem_jump_kernels(C.byref(ctx.ctx), variant)))
+                self._kernels[variant] = nk
             self.stats["jump_kernels"] += nk
             D._flip("dem")  # the plain step of the jump swapped both contact CSRs
             D._flip("bnd")
@@ -715,7 +722,11 @@ class LearnedRollout:
             if self.jump is not None and dev <= cfg.tol:
                 self.stats["learned_steps"] += m
                 self.stats["max_dev_accepted"] = max(self.stats["max_dev_accepted"], dev)
+                fresh = 1 if self.reuse_grid else 0
+                self.last_accepted = True
             else:
+                fresh = 0
+                self.last_accepted = False
                 _lib.check(lib.sphdem_jump_undo(C.byref(ctx.ctx), C.byref(self.jump or self._rebuild_jump()), st),
                            "sphdem_jump_undo")
                 self.stats["fallbacks"] += 1
