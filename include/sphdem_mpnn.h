@@ -215,6 +215,24 @@ int sphdem_jump_kernels(sphdem_ctx_t* ctx, int variant);
 /* Restore positions, velocities and fluid density saved by the last jump. */
 int sphdem_jump_undo(sphdem_ctx_t* ctx, const sphdem_jump_t* j, sphdem_stream_t stream);
 
+/* n_jumps jumps from first_step, judged on the device: each is the jump's
+ * graph plus a judge that, when *j->dev > tol (or a graph/kernel flag is
+ * set), runs the fallback in a conditional graph node -- undo, the m
+ * substeps as plain steps, a fluid re-bin -- so the host launches the jumps
+ * back to back and reads the outcome once.  stats (device int32[4], the
+ * caller zeroes it): jumps, fallbacks, largest accepted judge value (float
+ * bits), 1 if the last jump fell back.  Every jump runs 1 plain step (plus m
+ * for a fallback): the DEM CSR parity flips that many times.  flags as for
+ * sphdem_jump.  Needs one eager sphdem_jump on the context first (kernel
+ * attributes are set there). */
+int sphdem_rollout(sphdem_ctx_t* ctx, const sphdem_params_t* p, const sphdem_jump_t* j, int first_step,
+                   int n_jumps, float tol, int32_t flags, int32_t* stats, sphdem_stream_t stream);
+
+/* Kernel nodes the rollout graphs of those jumps hold: of the jumps
+ * themselves (body = 0) or of their fallback bodies (body = 1); -1 if a graph
+ * has not been captured. */
+int64_t sphdem_rollout_kernels(sphdem_ctx_t* ctx, int first_step, int n_jumps, int32_t flags, int body);
+
 /* Tensor-core GEMM check: C[M,N] (FP32) = A[M,K] B[N,K]^T for BF16 row-major
  * A, B; K, N in {16, 128}. */
 int sphdem_mpnn_gemm(const uint16_t* a, const uint16_t* b, float* c, int32_t m, int32_t n, int32_t k,

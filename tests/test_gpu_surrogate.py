@@ -14,6 +14,8 @@
   a jump whose density moved by more than the judge's tolerance.
 * A jump after an accepted one reuses the fluid grid its judge built: that
   grid is exactly the re-bin of the current positions.
+* Jumps judged on the device (conditional graph node) that all fall back
+  reproduce the plain method bit for bit.
 """
 import numpy as np
 import pytest
@@ -113,3 +115,31 @@ def test_jump_after_an_accepted_one_reuses_a_current_grid(trained):
     _lib.check(ctx.lib.sphdem_grid_build(C.byref(ctx.ctx), KIND_SPH, C.byref(ctx.params), ctx.stream), "grid")
     torch.cuda.synchronize()
     assert torch.equal(order, b["order"]) and torch.equal(start, b["cell_start"])
+
+
+def test_device_judged_fallbacks_reproduce_the_plain_method(trained):
+    """With a judge that rejects every jump, each jump is undone on the device
+    and its steps replayed plain inside the rollout graph (conditional node):
+    the rollout then equals the plain method bit for bit, and the accounting
+    counts every jump as a fallback."""
+    import dataclasses
+
+    from warp_sph_gpt_gb300.batch import Case
+    from warp_sph_gpt_gb300.generate import config_small
+    from warp_sph_gpt_gb300.surrogate import LearnedRollout, Network
+
+    base = trained["net"]
+    net = Network(dataclasses.replace(base.cfg, tol=-1.0), "cuda", theta=base.theta.cpu().numpy())
+    plain = Case(config_small())
+    plain.run(0, 100)
+    case = Case(config_small())
+    ro = LearnedRollout(case, net)
+    stats = ro.run(0, 100)
+    torch.cuda.synchronize()
+    assert stats["jumps"] == 10 and stats["fallbacks"] == 10 and stats["learned_steps"] == 0
+    assert stats["plain_steps"] == 100
+    for a, b in ((plain.P.pos, case.P.pos), (plain.P.vel, case.P.vel), (plain.D.pos, case.D.pos),
+                 (plain.D.vel, case.D.vel), (plain.D.omega, case.D.omega)):
+        np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+    np.testing.assert_array_equal(plain.D.contact_dem_offset_old.cpu().numpy(),
+                                  case.D.contact_dem_offset_old.cpu().numpy())

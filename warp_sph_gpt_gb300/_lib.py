@@ -183,6 +183,9 @@ _SIGNATURES = {
     "sphdem_mpnn_gemm": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_void_p,
                           C.c_void_p], C.c_int),
     "sphdem_jump": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int32, C.c_void_p], C.c_int),
+    "sphdem_rollout": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_int, C.c_float, C.c_int32, C.c_void_p,
+                        C.c_void_p], C.c_int),
+    "sphdem_rollout_kernels": ([C.c_void_p, C.c_int, C.c_int, C.c_int32, C.c_int], C.c_int64),
     "sphdem_jump_undo": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_jump_kernels": ([C.c_void_p, C.c_int], C.c_int),
     "sphdem_mpnn_wgrad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p,

@@ -424,6 +424,25 @@ bool valid_ctx(const sphdem_ctx_t* c) {
 }
 
 }  // namespace
+namespace {
+
+// stats: [0] jumps, [1] fallbacks, [2] largest accepted judge value (float
+// bits; values are >= 0), [3] 1 if the last jump fell back.  One thread.
+__global__ void k_decide(const float* __restrict__ dev, const sphdem_ctl_t* __restrict__ gctl, float tol,
+                         cudaGraphConditionalHandle cond, int32_t* __restrict__ stats) {
+    const float d = *dev;
+    const bool fall = !(d <= tol) || gctl->status != 0;  // NaN, or a graph/kernel flag: fall back
+    stats[0] += 1;
+    if (fall)
+        stats[1] += 1;
+    else
+        stats[2] = max(stats[2], __float_as_int(d));
+    stats[3] = fall ? 1 : 0;
+    cudaGraphSetConditional(cond, fall ? 1u : 0u);
+}
+
+}  // namespace
+
 }  // namespace sd
 
 using namespace sd;
@@ -675,6 +694,166 @@ int sphdem_jump_undo(sphdem_ctx_t* c, const sphdem_jump_t* j, sphdem_stream_t st
     return jump_keep(c, j, true, as_stream(stream));
 }
 
+// ---------------------------------------------------------------------------
+// device-judged rollout: the jumps are replayed back to back with no host
+// round trip.  Each rollout graph is the jump's graph plus a judge kernel
+// that sets a conditional node: non-zero runs the fallback body (undo the
+// substeps, m plain steps, then the fluid re-bin the next jump relies on).
+// ---------------------------------------------------------------------------
+namespace {
+
+struct RolloutEntry {
+    sphdem_ctx_t snap;
+    sphdem_params_t params;
+    sphdem_jump_t jump;
+    float tol = 0.0f;
+    int32_t* stats = nullptr;
+    cudaStream_t cap = nullptr;
+    std::map<int, cudaGraphExec_t> exec;            // key: Shepard pattern of the K steps * 2 + fresh
+    std::map<int, std::pair<int, int>> kernels;     // key -> (jump graph, fallback body) kernel nodes
+};
+std::map<const sphdem_ctx_t*, RolloutEntry> g_rollouts;
+
+void drop_rollout(RolloutEntry& e) {
+    for (auto& kv : e.exec)
+        if (kv.second) cudaGraphExecDestroy(kv.second);
+    e.exec.clear();
+    e.kernels.clear();
+}
+
+int capture_err(const char* what, cudaError_t e) {
+    set_error(what, e);
+    return SPHDEM_ERR_CUDA;
+}
+
+// Capture the rollout graph of a jump starting at `step`.
+int capture_rollout(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, int step, bool fresh,
+                    float tol, int32_t* stats, cudaStream_t cap, cudaGraphExec_t* out, std::pair<int, int>* nk) {
+    const bool shep = shepard_due(p, step);
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) return capture_err("rollout capture begin", e);
+    cudaStreamCaptureStatus cs;
+    cudaGraph_t graph = nullptr;
+    cudaGraphConditionalHandle cond = 0;
+    e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, &graph);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&cond, graph, 0, cudaGraphCondAssignDefault);
+    int rc = e == cudaSuccess ? jump_body(c, p, j, shep, fresh, cap) : SPHDEM_ERR_CUDA;
+    cudaGraph_t body = nullptr;
+    if (!rc) {
+        k_decide<<<1, 1, 0, cap>>>(j->dev, j->graph_ctl, tol, cond, stats);
+        const cudaGraphNode_t* deps = nullptr;
+        size_t nd = 0;
+        e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 1;
+        cudaGraphNode_t node = nullptr;
+        if (e == cudaSuccess) e = cudaGraphAddNode(&node, graph, deps, nullptr, nd, &np);
+        if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(cap, &node, nullptr, 1,
+                                                                       cudaStreamSetCaptureDependencies);
+        if (e == cudaSuccess) body = np.conditional.phGraph_out[0];
+        if (e != cudaSuccess) rc = capture_err("rollout conditional", e);
+    }
+    cudaGraph_t done = nullptr;
+    e = cudaStreamEndCapture(cap, &done);
+    if (rc || e != cudaSuccess) {
+        if (done) cudaGraphDestroy(done);
+        return rc ? rc : capture_err("rollout capture end", e);
+    }
+    // the fallback body
+    e = cudaStreamBeginCaptureToGraph(cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+    if (e != cudaSuccess) {
+        cudaGraphDestroy(done);
+        return capture_err("rollout body capture", e);
+    }
+    rc = jump_keep(c, j, true, cap);
+    for (int s = 1; !rc && s <= j->substeps; ++s) rc = loop_body(c, p, shepard_due(p, step + s), 1, cap);
+    if (!rc) rc = build_grid(&c->grid_sph, c->sph.pos, c->ctl, cap);
+    cudaGraph_t body_done = nullptr;
+    e = cudaStreamEndCapture(cap, &body_done);
+    if (rc || e != cudaSuccess) {
+        cudaGraphDestroy(done);
+        return rc ? rc : capture_err("rollout body capture end", e);
+    }
+    nk->first = count_kernel_nodes(done) ;
+    nk->second = count_kernel_nodes(body);
+    e = cudaGraphInstantiate(out, done, 0);
+    cudaGraphDestroy(done);
+    if (e != cudaSuccess) return capture_err("rollout graph instantiate", e);
+    return SPHDEM_OK;
+}
+
+}  // namespace
+
+int sphdem_rollout(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, int first_step, int n_jumps,
+                   float tol, int32_t flags, int32_t* stats, sphdem_stream_t stream) {
+    if (!valid_ctx(c) || !p || !j || !j->keep || !j->dev || !j->graph_ctl || !j->scan_scratch || j->substeps < 1 ||
+        !stats || n_jumps < 0) {
+        set_error_msg("rollout: invalid arguments");
+        return SPHDEM_ERR_INVALID;
+    }
+    cudaStream_t st = as_stream(stream);
+    const int K = j->substeps + 1;
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    RolloutEntry& e = g_rollouts[c];
+    if (memcmp(&e.snap, c, sizeof(*c)) != 0 || memcmp(&e.params, p, sizeof(*p)) != 0 ||
+        memcmp(&e.jump, j, sizeof(*j)) != 0 || e.tol != tol || e.stats != stats) {
+        drop_rollout(e);
+        e.snap = *c;
+        e.params = *p;
+        e.jump = *j;
+        e.tol = tol;
+        e.stats = stats;
+    }
+    if (!e.cap) {
+        cudaError_t err = cudaStreamCreateWithFlags(&e.cap, cudaStreamNonBlocking);
+        if (err != cudaSuccess) return capture_err("rollout capture stream", err);
+    }
+    bool fresh = (flags & SPHDEM_JUMP_GRID_FRESH) != 0;
+    for (int i = 0; i < n_jumps; ++i) {
+        const int step = first_step + i * K;
+        int pattern = 0;
+        for (int s = 0; s < K; ++s) pattern |= shepard_due(p, step + s) ? (1 << s) : 0;
+        const int key = pattern * 2 + (fresh ? 1 : 0);
+        auto it = e.exec.find(key);
+        if (it == e.exec.end()) {
+            cudaGraphExec_t x = nullptr;
+            std::pair<int, int> nk(0, 0);
+            int rc = capture_rollout(c, p, j, step, fresh, tol, stats, e.cap, &x, &nk);
+            if (rc) return rc;
+            it = e.exec.emplace(key, x).first;
+            e.kernels[key] = nk;
+        }
+        cudaError_t err = cudaGraphLaunch(it->second, st);
+        if (err != cudaSuccess) return capture_err("rollout graph launch", err);
+        fresh = true;  // an accepted jump's judge, or the fallback body, re-binned the fluid
+    }
+    return SPHDEM_OK;
+}
+
+// Kernel nodes per rollout jump: accepted (body = 0) or fallback body (body = 1),
+// summed over the graphs captured for this context; -1 if none.
+int64_t sphdem_rollout_kernels(sphdem_ctx_t* c, int first_step, int n_jumps, int32_t flags, int body) {
+    std::lock_guard<std::mutex> lock(g_graph_mu);
+    auto it = g_rollouts.find(c);
+    if (it == g_rollouts.end()) return -1;
+    const RolloutEntry& e = it->second;
+    const int K = e.jump.substeps + 1;
+    bool fresh = (flags & SPHDEM_JUMP_GRID_FRESH) != 0;
+    int64_t total = 0;
+    for (int i = 0; i < n_jumps; ++i) {
+        int pattern = 0;
+        for (int s = 0; s < K; ++s) pattern |= shepard_due(&e.params, first_step + i * K + s) ? (1 << s) : 0;
+        auto k = e.kernels.find(pattern * 2 + (fresh ? 1 : 0));
+        if (k == e.kernels.end()) return -1;
+        total += body ? k->second.second : k->second.first;
+        fresh = true;
+    }
+    return total;
+}
+
 // Blocking helper: one loop body of run_forward (moving-grid rebuild + one
 // step) with a CUDA event between phases on the launch stream; fills ms[k]
 // with the duration of phase k (SPHDEM_PHASE_* order) and synchronises.
@@ -751,6 +930,12 @@ int sphdem_release(sphdem_ctx_t* c) {
             if (x) cudaGraphExecDestroy(x);
         if (jt->second.cap) cudaStreamDestroy(jt->second.cap);
         g_jumps.erase(jt);
+    }
+    auto rt = g_rollouts.find(c);
+    if (rt != g_rollouts.end()) {
+        drop_rollout(rt->second);
+        if (rt->second.cap) cudaStreamDestroy(rt->second.cap);
+        g_rollouts.erase(rt);
     }
     auto it = g_graphs.find(c);
     if (it == g_graphs.end()) return SPHDEM_OK;

@@ -628,10 +628,16 @@ def train(net: Network, ts: TrainingSet, members, iters: int, lr: float = 1e-3, 
 class LearnedRollout:
     """Advance a case with jumps of K = m + 1 steps (one plain, m learned).
 
-    Each jump is one call of sphdem_jump (a CUDA graph: plain step, network,
-    prior + correction, density judge); the host reads the judge's result and,
-    above ``tol`` (or on a graph-capacity overflow), undoes the jump and runs
-    the m steps with the plain method."""
+    Each jump is a CUDA graph: plain step, network, prior + correction,
+    density judge.  By default (``native``) the judge decides on the device:
+    a conditional node in the same graph undoes the jump and runs the m steps
+    with the plain method when the judge value is above ``tol`` (or a graph
+    capacity overflowed), so jumps are launched back to back and the host
+    reads the outcome once per chunk (sphdem_rollout).  The host-judged path
+    (sphdem_jump, the value read back after every jump) runs the first jump
+    and is kept as ``native = False``."""
+
+    CHUNK = 16  # jumps per device-judged launch sequence (one host read each)
 
     def __init__(self, case, net: Network, reuse_grid: bool = True):
         from .engine import context_for
@@ -650,6 +656,10 @@ class LearnedRollout:
         self.jump = None
         self._kernels = {}
         self.last_accepted = False  # the last jump of the last run() was accepted
+        self.native = True          # device-judged jumps (sphdem_rollout); False: host-judged
+        self._warm = False          # one host-judged jump has run (kernel attributes set)
+        self.dstats = torch.zeros(4, dtype=torch.int32, device=net.device)
+        self.hstats = torch.zeros(4, dtype=torch.int32).pin_memory()
         self.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0,
                           jump_kernels=0)
 
@@ -676,6 +686,71 @@ class LearnedRollout:
         self.jump = j
 
     def run(self, first_step: int, n_steps: int) -> dict:
+        """Advance n_steps from first_step: jumps judged on the device
+        (sphdem_rollout: launched back to back, the fallback inside the graph),
+        in chunks of CHUNK jumps with one host read each; the first jump of a
+        rollout goes through the host-judged path (it sets kernel attributes
+        eagerly), steps short of a jump run plain."""
+        c, cfg, lib = self.case, self.cfg, self.lib
+        m, K = cfg.substeps, cfg.substeps + 1
+        if self.jump is None:
+            self._setup()
+        ctx, D = self.ctx, c.D
+        step, end = first_step, first_step + n_steps
+        ctx.set_params(c.solv, c.scales)  # constant over the rollout (the plain fallback sets its own)
+        fresh = 0  # the caller may have moved or restored the state: re-bin in the first jump
+        if not self._warm and end - step >= K:
+            fresh = self._run_hosted(step, K, fresh)
+            self._warm = True
+            step += K
+        st = self.g.stream()
+        while self.native and end - step >= K:
+            n = min((end - step) // K, self.CHUNK)
+            self.dstats.zero_()
+            _lib.check(lib.sphdem_rollout(C.byref(ctx.ctx), C.byref(ctx.params), C.byref(self.jump), step, n,
+                                          float(cfg.tol), fresh, C.c_void_p(self.dstats.data_ptr()), st),
+                       "sphdem_rollout")
+            k_jump = int(lib.sphdem_rollout_kernels(C.byref(ctx.ctx), step, n, fresh, 0))
+            k_body = int(lib.sphdem_rollout_kernels(C.byref(ctx.ctx), step, n, fresh, 1))
+            self.hstats.copy_(self.dstats, non_blocking=True)
+            self.host[1:2].copy_(self.g.ctl[3:4], non_blocking=True)
+            self.host[2:3].copy_(ctx.ctl[3:4], non_blocking=True)
+            torch.cuda.current_stream(self.net.device).synchronize()
+            jumps, fb, maxbits, last = (int(v) for v in self.hstats.tolist())
+            if (n + m * fb) % 2:  # each plain step swapped both contact CSRs
+                D._flip("dem")
+                D._flip("bnd")
+            s = self.stats
+            s["jumps"] += jumps
+            s["fallbacks"] += fb
+            s["plain_steps"] += jumps + m * fb
+            s["learned_steps"] += m * (jumps - fb)
+            s["max_dev_accepted"] = max(s["max_dev_accepted"], float(np.array(maxbits, np.int32).view(np.float32)))
+            s["jump_kernels"] += max(k_jump, 0) + (max(k_body, 0) * fb) // max(n, 1)
+            gflags, cflags = int(self.host[1]), int(self.host[2])
+            if cflags:
+                ctx._raise_for(cflags)
+            if gflags & 0x8:  # edge capacity: those jumps fell back; grow and re-capture
+                self.g.ctl[3] = 0
+                self.g._alloc_edges(int(self.g.capacity * 1.5))
+                self._setup()
+            elif gflags:
+                raise RuntimeError(f"learned jump raised device status 0x{gflags:x}")
+            self.last_accepted = not last
+            fresh = 1 if self.reuse_grid else 0  # the judge or the fallback body re-binned the fluid
+            step += n * K
+        if not self.native and end - step >= K:
+            fresh = self._run_hosted(step, (end - step) // K * K, fresh)
+            step = end - (end - step) % K
+        if step < end:
+            c.run(step, end - step)
+            self.stats["plain_steps"] += end - step
+            self.last_accepted = False
+        return dict(self.stats)
+
+    def _run_hosted(self, first_step: int, n_steps: int, fresh: int) -> int:
+        """Jumps judged on the host: one sphdem_jump per jump, the judge value read
+        back, undo + plain steps above tolerance.  Returns the grid-fresh flag."""
         c, cfg, lib = self.case, self.cfg, self.lib
         m, K = cfg.substeps, cfg.substeps + 1
         if self.jump is None:
@@ -683,13 +758,12 @@ class LearnedRollout:
         ctx, D = self.ctx, c.D
         step, end = first_step, first_step + n_steps
         st = self.g.stream()
-        ctx.set_params(c.solv, c.scales)  # constant over the rollout (the plain fallback sets its own)
-        fresh = 0  # SPHDEM_JUMP_GRID_FRESH: the last call here was an accepted jump
         while step < end:
             if end - step < K:
                 c.run(step, end - step)
                 self.stats["plain_steps"] += end - step
                 self.last_accepted = False
+                fresh = 0
                 break
             _lib.check(lib.sphdem_jump(C.byref(ctx.ctx), C.byref(ctx.params), C.byref(self.jump), step, fresh, st),
                        "sphdem_jump")
@@ -733,7 +807,7 @@ class LearnedRollout:
                 c.run(step + 1, m)
                 self.stats["plain_steps"] += m
             step += K
-        return dict(self.stats)
+        return fresh
 
     def _rebuild_jump(self):
         self._setup()
