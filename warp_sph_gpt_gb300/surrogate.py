@@ -637,7 +637,7 @@ class LearnedRollout:
     (sphdem_jump, the value read back after every jump) runs the first jump
     and is kept as ``native = False``."""
 
-    CHUNK = 16  # jumps per device-judged launch sequence (one host read each)
+    CHUNK = 50  # jumps per device-judged launch sequence (one host read each)
 
     def __init__(self, case, net: Network, reuse_grid: bool = True):
         from .engine import context_for
