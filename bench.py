@@ -331,6 +331,8 @@ def gpu_arm(args, rank, world, local_rank):
         tuning = {"lanes_sph": args.lanes_sph or default_lanes(runner.P.n)}
         if args.porosity_variant >= 0:
             tuning["porosity_variant"] = args.porosity_variant
+        if args.nbr_cap >= 0:
+            tuning["nbr_cap"] = args.nbr_cap
     runner.tune(tuning)
     gen, solv, desc = runner.gen, runner.solv, runner.desc
     P, B, D, W = runner.P, runner.B, runner.D, runner.W
@@ -829,6 +831,9 @@ def main():
                     help="porosity normaliser implementation (-1 = library default)")
     ap.add_argument("--lanes-sph", type=int, default=0, choices=(0, 1, 32),
                     help="threads per particle of the SPH loops (0 = by system size)")
+    ap.add_argument("--nbr-cap", type=int, default=-1,
+                    help="neighbour-list capacity between the density and force passes (-1 = sized by the "
+                         "library, 0 = no lists)")
     ap.add_argument("--cell-factor", type=float, default=1.0,
                     help="fluid/wall cell width as a fraction of the SPH support")
     args = ap.parse_args()
