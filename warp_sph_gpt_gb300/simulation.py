@@ -42,18 +42,11 @@ def SPHDEM_OneStep(solv, P_sph, P_bnd, P_dem, P_dem_bnd, grid_sph, grid_bnd, gri
     """One coupled step at a common time level (source/Simulation.py:102-221):
     SPH fields and forces -> DEM-DEM and DEM-wall contacts with CSR history
     rebuild and swap -> porosity and -grad p -> fluid-to-DEM pressure and drag
-    -> drag reaction on the fluid -> SPH and DEM integration."""
-    scales = dem_search_scales(P_dem, P_dem_bnd) if search_scales is None else search_scales
-    ctx = context_for(P_sph, P_bnd, P_dem, P_dem_bnd, (grid_sph, grid_bnd, grid_dem, grid_dem_bnd))
-    ctx.set_params(solv, scales)
-    ctx.poll_status()
-    ctx.prepare(rebuild_moving=True, wall_key=(float(C.c_float(solv.support).value),
-                                               float(C.c_float(solv.h).value)))
-    _lib.check(ctx.lib.sphdem_sphdem_onestep(C.byref(ctx.ctx), C.byref(ctx.params), int(step), ctx.stream),
-               "SPHDEM_OneStep")
-    P_dem._flip("dem")
-    P_dem._flip("bnd")
-    ctx.post_status()
+    -> drag reaction on the fluid -> SPH and DEM integration.  The moving grids
+    are re-binned inside the step; the step is replayed from the same CUDA
+    graph as run_steps (one per Shepard cadence variant)."""
+    run_steps(solv, P_sph, P_bnd, grid_sph, grid_bnd, P_dem, P_dem_bnd, grid_dem, grid_dem_bnd, first_step=step,
+              n_steps=1, search_scales=search_scales)
 
 
 def run_steps(solv, P_sph, P_bnd, grid_sph, grid_bnd, P_dem=None, P_dem_bnd=None, grid_dem=None,
