@@ -378,4 +378,29 @@ void set_error_msg(const char* msg);
 int launch_status(const char* where);
 inline cudaStream_t as_stream(sphdem_stream_t s) { return (cudaStream_t)s; }
 inline int blocks_for(long n, int threads) { return (int)((n + threads - 1) / threads); }
+
+// Programmatic dependent launch: a step kernel is launched with programmatic
+// stream serialization, so the GPU may schedule it while the previous kernel
+// on the stream is still finishing; every such kernel calls pdl_wait() first
+// (griddepcontrol.wait: blocks until the preceding grids have completed and
+// their writes are visible -- the ordinary stream order, minus the launch gap)
+// and pdl_launch() to let its own successor be scheduled.  Both are no-ops
+// for an ordinary launch.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... P, typename... A>
+inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, A&&... args) {
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);  // errors surface through launch_status
+}
 }  // namespace sd

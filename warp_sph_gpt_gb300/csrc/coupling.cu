@@ -40,6 +40,8 @@ __device__ float drag_beta(float eps, float rho, float mu, float diameter, float
 
 __global__ void k_drag_beta(const float* eps, const float* rho, const float* mu, const float* d, const float* speed,
                             int n, float* out) {
+    pdl_wait();
+    pdl_launch();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) out[i] = drag_beta(eps[i], rho[i], mu[i], d[i], speed[i]);
 }
@@ -108,6 +110,8 @@ __device__ __forceinline__ float ball_weight_h(float px, float py, float pz, con
 // keeps slot order inside each block of 256 slots (ordered block compaction),
 // so consecutive entries are neighbours in space.
 __global__ void __launch_bounds__(256) k_near(CplArgs a) {
+    pdl_wait();
+    pdl_launch();
     __shared__ int warp_tot[8];
     __shared__ int base;
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -208,6 +212,8 @@ __device__ __forceinline__ float porosity_solid(const CplArgs& a, const float4& 
 // takes an entry does not change its result.
 template <bool UNIFORM>
 __global__ void __launch_bounds__(256) k_porosity_near(CplArgs a) {
+    pdl_wait();
+    pdl_launch();
     const int lane = threadIdx.x & 31;
     const int n_near = a.ctl->n_near;
     for (;;) {
@@ -304,6 +310,8 @@ __device__ __forceinline__ int tile_fill(TileShared& sh, int b, int m, int& r, i
 }
 
 __global__ void __launch_bounds__(kTileThreads, 3) k_porosity_tiles(CplArgs a) {
+    pdl_wait();
+    pdl_launch();
     __shared__ TileShared sh;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
@@ -444,6 +452,8 @@ constexpr int kIdThreads = 256;
 
 // Kernel_interaction_dem: one CTA per DEM a.
 __global__ void __launch_bounds__(kIdThreads) k_interaction_dem(CplArgs a) {
+    pdl_wait();
+    pdl_launch();
     __shared__ float red[kIdThreads / 32][8];
     const int am = blockIdx.x;
     const float3 pa = ld3(a.D.pos, am);
@@ -529,6 +539,8 @@ __global__ void __launch_bounds__(kIdThreads) k_interaction_dem(CplArgs a) {
 // Kernel_interaction_sph (+ Kernel_step_sph when INTEGRATE), point order.
 template <bool INTEGRATE>
 __global__ void k_react(CplArgs a) {
+    pdl_wait();
+    pdl_launch();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.P.n) return;
     const float3 pi = ld3(a.P.pos, i);
@@ -599,7 +611,7 @@ int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, f
         set_error("porosity memset", e);
         return SPHDEM_ERR_CUDA;
     }
-    k_near<<<blocks_for(n, 256), 256, 0, st>>>(a);
+    launch_pdl(k_near, blocks_for(n, 256), 256, 0, st, a);
     if (c->dem.n > 0) {
         int dev = 0, sms = 148;
         cudaGetDevice(&dev);
@@ -612,15 +624,15 @@ int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, f
             const int need = blocks_for(n, kGroup);
             int blocks = sms * 4;  // resident CTAs of k_porosity_tiles per SM
             if (need < blocks) blocks = need;
-            k_porosity_tiles<<<blocks, kTileThreads, 0, st>>>(a);
+            launch_pdl(k_porosity_tiles, blocks, kTileThreads, 0, st, a);
         } else {
             const int need = blocks_for(n, 8);
             int blocks = sms * 8;
             if (need < blocks) blocks = need;
             if (a.h > 0.0f)
-                k_porosity_near<true><<<blocks, 256, 0, st>>>(a);
+                launch_pdl(k_porosity_near<true>, blocks, 256, 0, st, a);
             else
-                k_porosity_near<false><<<blocks, 256, 0, st>>>(a);
+                launch_pdl(k_porosity_near<false>, blocks, 256, 0, st, a);
         }
     }
     return launch_status("porosity");
@@ -633,7 +645,7 @@ int run_interaction_dem(const sphdem_ctx_t* c, float mu, float eps_min, float ep
     a.eps_min = eps_min;
     a.eps_max = eps_max;
     a.dt = dt;
-    k_interaction_dem<<<c->dem.n, kIdThreads, 0, st>>>(a);
+    launch_pdl(k_interaction_dem, c->dem.n, kIdThreads, 0, st, a);
     return launch_status("interaction_dem");
 }
 
@@ -643,16 +655,16 @@ int run_react(const sphdem_ctx_t* c, float support, float dt, bool integrate, cu
     CplArgs a = make_args(c, support, 0.0f);
     a.dt = dt;
     if (integrate)
-        k_react<true><<<blocks_for(n, 256), 256, 0, st>>>(a);
+        launch_pdl(k_react<true>, blocks_for(n, 256), 256, 0, st, a);
     else
-        k_react<false><<<blocks_for(n, 256), 256, 0, st>>>(a);
+        launch_pdl(k_react<false>, blocks_for(n, 256), 256, 0, st, a);
     return launch_status("react");
 }
 
 int run_drag_beta(const float* eps, const float* rho, const float* mu, const float* d, const float* speed, int n,
                   float* out, cudaStream_t st) {
     if (n <= 0) return SPHDEM_OK;
-    k_drag_beta<<<blocks_for(n, 256), 256, 0, st>>>(eps, rho, mu, d, speed, n, out);
+    launch_pdl(k_drag_beta, blocks_for(n, 256), 256, 0, st, eps, rho, mu, d, speed, n, out);
     return launch_status("drag_beta");
 }
 

@@ -189,6 +189,8 @@ __device__ void fill_row(const DemArgs& A, int a, const sphdem_csr_t& old, const
 
 // Single-CTA rebuild of the selected contact CSR kinds.
 __global__ void __launch_bounds__(kDemThreads) k_contacts(DemArgs A) {
+    pdl_wait();
+    pdl_launch();
     __shared__ int warp_tot[kDemThreads / 32];
     const int n = A.D.n;
     const int old_d = A.ctl->old_dem, old_b = A.ctl->old_bnd;
@@ -252,6 +254,8 @@ __global__ void __launch_bounds__(kDemThreads) k_contacts(DemArgs A) {
 
 // Per-DEM coupling constants: 1/h, 21/(16 pi h^3), sqrt bound of 2h, 2h.
 __global__ void k_dem_aux(const float* __restrict__ h, int n, float4* __restrict__ aux) {
+    pdl_wait();
+    pdl_launch();
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= n) return;
     const float hb = h[a];
@@ -261,6 +265,8 @@ __global__ void k_dem_aux(const float* __restrict__ h, int n, float4* __restrict
 
 // Kernel_step_dem (kernel/KERNEL_DEM_step.py:6-30), every operation rounded.
 __global__ void k_step_dem(sphdem_dem_t D, float dt) {
+    pdl_wait();
+    pdl_launch();
     const int a = blockIdx.x * blockDim.x + threadIdx.x;
     if (a >= D.n) return;
     const float m = D.m[a], I = D.inertia[a];
@@ -292,19 +298,19 @@ int run_contacts(const sphdem_ctx_t* c, float radius_max, float bnd_radius_max, 
     A.g = g;
     A.dt = dt;
     A.which = which;
-    k_contacts<<<1, kDemThreads, 0, st>>>(A);
+    launch_pdl(k_contacts, 1, kDemThreads, 0, st, A);
     return launch_status("contacts");
 }
 
 int run_dem_aux(const sphdem_ctx_t* c, cudaStream_t st) {
     if (c->dem.n <= 0) return SPHDEM_OK;
-    k_dem_aux<<<blocks_for(c->dem.n, 128), 128, 0, st>>>(c->dem.h, c->dem.n, (float4*)c->work.dem_aux);
+    launch_pdl(k_dem_aux, blocks_for(c->dem.n, 128), 128, 0, st, c->dem.h, c->dem.n, (float4*)c->work.dem_aux);
     return launch_status("dem_aux");
 }
 
 int run_step_dem(const sphdem_ctx_t* c, float dt, cudaStream_t st) {
     if (c->dem.n <= 0) return SPHDEM_OK;
-    k_step_dem<<<blocks_for(c->dem.n, 128), 128, 0, st>>>(c->dem, dt);
+    launch_pdl(k_step_dem, blocks_for(c->dem.n, 128), 128, 0, st, c->dem, dt);
     return launch_status("step_dem");
 }
 

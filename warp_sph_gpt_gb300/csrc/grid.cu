@@ -27,6 +27,8 @@ constexpr int kScanTile = kScanThreads * kScanItems;  // 1024 cells per tile
 __global__ void k_bin(const float* __restrict__ pos, int n, const int* __restrict__ inst, int lo0, int lo1,
                       int lo2, int d0, int d1, int d2, float inv, int ncl, int* __restrict__ key,
                       int* __restrict__ count, sphdem_ctl_t* ctl) {
+    pdl_wait();
+    pdl_launch();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     float x = pos[3 * i], y = pos[3 * i + 1], z = pos[3 * i + 2];
@@ -39,6 +41,8 @@ __global__ void k_bin(const float* __restrict__ pos, int n, const int* __restric
 
 // Each block scans one tile in place (exclusive) and records its total.
 __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(int* __restrict__ data, int n, int* __restrict__ sums) {
+    pdl_wait();
+    pdl_launch();
     __shared__ int warp_tot[kScanThreads / 32];
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -60,6 +64,8 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(int* __restrict__ d
 
 // One block: exclusive scan of nb tile totals in place; sums[nb] = grand total.
 __global__ void __launch_bounds__(1024) k_scan_sums(int* __restrict__ sums, int nb) {
+    pdl_wait();
+    pdl_launch();
     __shared__ int warp_tot[32];
     int carry = 0;
     for (int base = 0; base < nb; base += blockDim.x) {
@@ -74,6 +80,8 @@ __global__ void __launch_bounds__(1024) k_scan_sums(int* __restrict__ sums, int 
 }
 
 __global__ void k_scan_add(int* __restrict__ data, int n, const int* __restrict__ sums, int total_points) {
+    pdl_wait();
+    pdl_launch();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) data[i] += sums[i / kScanTile];
     if (i == 0) data[n] = total_points;
@@ -81,6 +89,8 @@ __global__ void k_scan_add(int* __restrict__ data, int n, const int* __restrict_
 
 // As k_scan_add, with data[n] = the grand total left by k_scan_sums.
 __global__ void k_scan_add_total(int* __restrict__ data, int n, const int* __restrict__ sums, int nb) {
+    pdl_wait();
+    pdl_launch();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) data[i] += sums[i / kScanTile];
     if (i == 0) data[n] = sums[nb];
@@ -88,6 +98,8 @@ __global__ void k_scan_add_total(int* __restrict__ data, int n, const int* __res
 
 __global__ void k_scatter(const int* __restrict__ key, int n, const int* __restrict__ start, int* __restrict__ cursor,
                           int* __restrict__ order) {
+    pdl_wait();
+    pdl_launch();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int k = key[i];
@@ -145,6 +157,8 @@ __device__ __forceinline__ void sort_cells_warp(const int* __restrict__ start, i
 }
 
 __global__ void k_sort_cells(const int* __restrict__ start, int ncell, int* __restrict__ order) {
+    pdl_wait();
+    pdl_launch();
     sort_cells_warp(start, ncell, order, (blockIdx.x * blockDim.x + threadIdx.x) & ~31);
 }
 
@@ -163,6 +177,8 @@ __global__ void __launch_bounds__(kOneThreads) k_build_one(const float* __restri
                                                           int* __restrict__ key, int* __restrict__ start,
                                                           int* __restrict__ cursor, int* __restrict__ order,
                                                           sphdem_ctl_t* ctl) {
+    pdl_wait();
+    pdl_launch();
     __shared__ int warp_tot[kOneThreads / 32];
     const int tid = threadIdx.x;
     for (int c = tid; c <= ncell; c += kOneThreads) start[c] = 0;
@@ -203,6 +219,8 @@ __global__ void k_gather_fluid(const int* __restrict__ order, int n, const float
                                const float* __restrict__ m, const float* __restrict__ vel,
                                const float* __restrict__ rho, float4* __restrict__ posm, float4* __restrict__ velo,
                                float* __restrict__ vprev) {
+    pdl_wait();
+    pdl_launch();
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     int o = order[k];
@@ -213,6 +231,8 @@ __global__ void k_gather_fluid(const int* __restrict__ order, int n, const float
 
 __global__ void k_gather_vol(const int* __restrict__ order, int n, const float* __restrict__ m,
                              const float* __restrict__ rho, float* __restrict__ out) {
+    pdl_wait();
+    pdl_launch();
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k < n) {
         int o = order[k];
@@ -225,6 +245,8 @@ __global__ void k_gather_vol(const int* __restrict__ order, int n, const float* 
 // never move, so this sum is a constant of the wall grid and is cached here.
 __global__ void k_wall_self(Geo gb, const float4* __restrict__ posm, int n, float s2, float rq, Kern kern,
                             float* __restrict__ self) {
+    pdl_wait();
+    pdl_launch();
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     float4 p = posm[k];
@@ -243,9 +265,9 @@ __global__ void k_wall_self(Geo gb, const float4* __restrict__ posm, int n, floa
 int scan_cells(int* data, int ncell, int total_points, int* sums, cudaStream_t st) {
     int nb = (ncell + kScanTile - 1) / kScanTile;
     if (nb < 1) nb = 1;
-    k_scan_tiles<<<nb, kScanThreads, 0, st>>>(data, ncell, sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(sums, nb);
-    k_scan_add<<<blocks_for(ncell > 0 ? ncell : 1, 256), 256, 0, st>>>(data, ncell, sums, total_points);
+    launch_pdl(k_scan_tiles, nb, kScanThreads, 0, st, data, ncell, sums);
+    launch_pdl(k_scan_sums, 1, 1024, 0, st, sums, nb);
+    launch_pdl(k_scan_add, blocks_for(ncell > 0 ? ncell : 1, 256), 256, 0, st, data, ncell, sums, total_points);
     return launch_status("scan_cells");
 }
 
@@ -255,9 +277,9 @@ int scan_cells(int* data, int ncell, int total_points, int* sums, cudaStream_t s
 int scan_counts(int* data, int n, int* sums, cudaStream_t st) {
     int nb = (n + kScanTile - 1) / kScanTile;
     if (nb < 1) nb = 1;
-    k_scan_tiles<<<nb, kScanThreads, 0, st>>>(data, n, sums);
-    k_scan_sums<<<1, 1024, 0, st>>>(sums, nb);
-    k_scan_add_total<<<blocks_for(n > 0 ? n : 1, 256), 256, 0, st>>>(data, n, sums, nb);
+    launch_pdl(k_scan_tiles, nb, kScanThreads, 0, st, data, n, sums);
+    launch_pdl(k_scan_sums, 1, 1024, 0, st, sums, nb);
+    launch_pdl(k_scan_add_total, blocks_for(n > 0 ? n : 1, 256), 256, 0, st, data, n, sums, nb);
     return launch_status("scan_counts");
 }
 
@@ -270,7 +292,7 @@ int build_grid(sphdem_grid_t* g, const float* pos, sphdem_ctl_t* ctl, cudaStream
     }
     const int n = g->n;
     if (n <= kOneMaxPoints && ncell <= kOneMaxCells) {
-        k_build_one<<<1, kOneThreads, 0, st>>>(pos, n, g->inst, g->lo[0], g->lo[1], g->lo[2], g->dim[0], g->dim[1],
+        launch_pdl(k_build_one, 1, kOneThreads, 0, st, pos, n, g->inst, g->lo[0], g->lo[1], g->lo[2], g->dim[0], g->dim[1],
                                                g->dim[2], g->inv_cell, g->ncell_local, ncell, g->key, g->cell_start,
                                                g->cursor, g->order, ctl);
         return launch_status("build_grid");
@@ -282,14 +304,14 @@ int build_grid(sphdem_grid_t* g, const float* pos, sphdem_ctl_t* ctl, cudaStream
         return SPHDEM_ERR_CUDA;
     }
     if (n > 0)
-        k_bin<<<blocks_for(n, 256), 256, 0, st>>>(pos, n, g->inst, g->lo[0], g->lo[1], g->lo[2], g->dim[0],
+        launch_pdl(k_bin, blocks_for(n, 256), 256, 0, st, pos, n, g->inst, g->lo[0], g->lo[1], g->lo[2], g->dim[0],
                                                   g->dim[1], g->dim[2], g->inv_cell, g->ncell_local, g->key,
                                                   g->cell_start, ctl);
     int rc = scan_cells(g->cell_start, ncell, n, g->block_sums, st);
     if (rc) return rc;
     if (n > 0) {
-        k_scatter<<<blocks_for(n, 256), 256, 0, st>>>(g->key, n, g->cell_start, g->cursor, g->order);
-        k_sort_cells<<<blocks_for(ncell, 256), 256, 0, st>>>(g->cell_start, ncell, g->order);
+        launch_pdl(k_scatter, blocks_for(n, 256), 256, 0, st, g->key, n, g->cell_start, g->cursor, g->order);
+        launch_pdl(k_sort_cells, blocks_for(ncell, 256), 256, 0, st, g->cell_start, ncell, g->order);
     }
     return launch_status("build_grid");
 }
@@ -297,7 +319,7 @@ int build_grid(sphdem_grid_t* g, const float* pos, sphdem_ctl_t* ctl, cudaStream
 int gather_fluid(const sphdem_ctx_t* c, cudaStream_t st) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
-    k_gather_fluid<<<blocks_for(n, 256), 256, 0, st>>>(c->grid_sph.order, n, c->sph.pos, c->sph.m, c->sph.vel,
+    launch_pdl(k_gather_fluid, blocks_for(n, 256), 256, 0, st, c->grid_sph.order, n, c->sph.pos, c->sph.m, c->sph.vel,
                                                       c->sph.rho, (float4*)c->work.f_posm,
                                                       (float4*)c->work.f_vel, c->work.f_vprev);
     return launch_status("gather_fluid");
@@ -307,11 +329,11 @@ int gather_wall(const sphdem_ctx_t* c, float support, float h, cudaStream_t st) 
     const int n = c->bnd.n;
     if (n <= 0) return SPHDEM_OK;
     // Same gather as the fluid (x, y, z, m), then the wall self density.
-    k_gather_fluid<<<blocks_for(n, 256), 256, 0, st>>>(c->grid_bnd.order, n, c->bnd.pos, c->bnd.m, c->bnd.vel,
+    launch_pdl(k_gather_fluid, blocks_for(n, 256), 256, 0, st, c->grid_bnd.order, n, c->bnd.pos, c->bnd.m, c->bnd.vel,
                                                       c->bnd.rho, (float4*)c->work.b_posm,
                                                       (float4*)c->work.b_vel, c->work.b_vprev);
     Geo gb = make_geo(c->grid_bnd);
-    k_wall_self<<<blocks_for(n, 128), 128, 0, st>>>(gb, (const float4*)c->work.b_posm, n, support * support,
+    launch_pdl(k_wall_self, blocks_for(n, 128), 128, 0, st, gb, (const float4*)c->work.b_posm, n, support * support,
                                                     pad_radius(support), make_kern(h), c->work.b_self);
     return launch_status("gather_wall");
 }
@@ -319,7 +341,7 @@ int gather_wall(const sphdem_ctx_t* c, float support, float h, cudaStream_t st) 
 int gather_wall_rho(const sphdem_ctx_t* c, cudaStream_t st) {
     const int n = c->bnd.n;
     if (n <= 0) return SPHDEM_OK;
-    k_gather_vol<<<blocks_for(n, 256), 256, 0, st>>>(c->grid_bnd.order, n, c->bnd.m, c->bnd.rho, c->work.b_vprev);
+    launch_pdl(k_gather_vol, blocks_for(n, 256), 256, 0, st, c->grid_bnd.order, n, c->bnd.m, c->bnd.rho, c->work.b_vprev);
     return launch_status("gather_wall_rho");
 }
 

@@ -83,6 +83,8 @@ struct DensArgs {
 
 template <int LANES, bool FLT, bool RHO, bool PRES>
 __global__ void __launch_bounds__(256) k_density(DensArgs a) {
+    pdl_wait();
+    pdl_launch();
     int lane;
     const int k = subject_index<LANES>(lane);
     if (k >= a.n) return;
@@ -159,6 +161,8 @@ struct WallArgs {
 
 template <int LANES, bool PRES>
 __global__ void __launch_bounds__(256) k_density_wall(WallArgs a) {
+    pdl_wait();
+    pdl_launch();
     int lane;
     const int k = subject_index<LANES>(lane);
     if (k >= a.n) return;
@@ -234,6 +238,8 @@ __device__ __forceinline__ void force_pair(const ForceArgs& a, const D2& r, cons
 
 template <int LANES, int MODE>
 __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
+    pdl_wait();
+    pdl_launch();
     int lane;
     const int k = subject_index<LANES>(lane);
     if (k >= a.n) return;
@@ -318,6 +324,8 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
 
 __global__ void k_pres(const float* __restrict__ rho, float* __restrict__ pres, int n, float rho0, float B,
                        float gamma) {
+    pdl_wait();
+    pdl_launch();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) pres[i] = tait(rho[i], rho0, B, gamma);
 }
@@ -326,6 +334,8 @@ __global__ void k_pres(const float* __restrict__ rho, float* __restrict__ pres, 
 
 namespace {
 __global__ void k_step_sph(float* pos, float* vel, const float* __restrict__ acc, int n, float dt) {
+    pdl_wait();
+    pdl_launch();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) euler_store(pos, vel, i, ld3(acc, i), dt);
 }
@@ -366,27 +376,27 @@ int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rh
     if (lanes == 32) {
         const int nb = blocks_for((long)n * 32, bs);
         if (flt && rho && pres)
-            k_density<32, true, true, true><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<32, true, true, true>, nb, bs, 0, st, a);
         else if (!flt && rho && pres)
-            k_density<32, false, true, true><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<32, false, true, true>, nb, bs, 0, st, a);
         else if (flt && !rho)
-            k_density<32, true, false, false><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<32, true, false, false>, nb, bs, 0, st, a);
         else if (!flt && rho && !pres)
-            k_density<32, false, true, false><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<32, false, true, false>, nb, bs, 0, st, a);
         else
-            k_density<32, true, true, false><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<32, true, true, false>, nb, bs, 0, st, a);
     } else {
         const int nb = blocks_for(n, bs);
         if (flt && rho && pres)
-            k_density<1, true, true, true><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<1, true, true, true>, nb, bs, 0, st, a);
         else if (!flt && rho && pres)
-            k_density<1, false, true, true><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<1, false, true, true>, nb, bs, 0, st, a);
         else if (flt && !rho)
-            k_density<1, true, false, false><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<1, true, false, false>, nb, bs, 0, st, a);
         else if (!flt && rho && !pres)
-            k_density<1, false, true, false><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<1, false, true, false>, nb, bs, 0, st, a);
         else
-            k_density<1, true, true, false><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density<1, true, true, false>, nb, bs, 0, st, a);
     }
     return launch_status("density");
 }
@@ -416,14 +426,14 @@ int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, f
     if (lanes == 32) {
         const int nb = blocks_for((long)n * 32, bs);
         if (pres)
-            k_density_wall<32, true><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density_wall<32, true>, nb, bs, 0, st, a);
         else
-            k_density_wall<32, false><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_density_wall<32, false>, nb, bs, 0, st, a);
     } else {
         if (pres)
-            k_density_wall<1, true><<<blocks_for(n, bs), bs, 0, st>>>(a);
+            launch_pdl(k_density_wall<1, true>, blocks_for(n, bs), bs, 0, st, a);
         else
-            k_density_wall<1, false><<<blocks_for(n, bs), bs, 0, st>>>(a);
+            launch_pdl(k_density_wall<1, false>, blocks_for(n, bs), bs, 0, st, a);
     }
     return launch_status("density_wall");
 }
@@ -458,33 +468,33 @@ int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, 
     if (lanes == 32) {
         const int nb = blocks_for((long)n * 32, bs);
         if (mode == 3)
-            k_force<32, 3><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_force<32, 3>, nb, bs, 0, st, a);
         else if (mode == 2)
-            k_force<32, 2><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_force<32, 2>, nb, bs, 0, st, a);
         else
-            k_force<32, 1><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_force<32, 1>, nb, bs, 0, st, a);
     } else {
         const int nb = blocks_for(n, bs);
         if (mode == 3)
-            k_force<1, 3><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_force<1, 3>, nb, bs, 0, st, a);
         else if (mode == 2)
-            k_force<1, 2><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_force<1, 2>, nb, bs, 0, st, a);
         else
-            k_force<1, 1><<<nb, bs, 0, st>>>(a);
+            launch_pdl(k_force<1, 1>, nb, bs, 0, st, a);
     }
     return launch_status("force");
 }
 
 int run_pres(const float* rho, float* pres, int n, float rho0, float c0, float gamma, cudaStream_t st) {
     if (n <= 0) return SPHDEM_OK;
-    k_pres<<<blocks_for(n, 256), 256, 0, st>>>(rho, pres, n, rho0, tait_B(rho0, c0, gamma), gamma);
+    launch_pdl(k_pres, blocks_for(n, 256), 256, 0, st, rho, pres, n, rho0, tait_B(rho0, c0, gamma), gamma);
     return launch_status("pres");
 }
 
 int run_step_sph(const sphdem_ctx_t* c, float dt, cudaStream_t st) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
-    k_step_sph<<<blocks_for(n, 256), 256, 0, st>>>(c->sph.pos, c->sph.vel, c->sph.acc, n, dt);
+    launch_pdl(k_step_sph, blocks_for(n, 256), 256, 0, st, c->sph.pos, c->sph.vel, c->sph.acc, n, dt);
     return launch_status("step_sph");
 }
 
