@@ -163,6 +163,8 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
                                              const float* __restrict__ bias, float* __restrict__ out_f32,
                                              uint16_t* __restrict__ out_bf, float* __restrict__ z_out,
                                              int32_t* status, const int* __restrict__ list, int n_direct) {
+    pdl_wait();
+    pdl_launch();
     constexpr uint32_t kB = N * K * 2, kA = kT * K * 2;
     constexpr uint32_t kCols = N < 32 ? 32 : N;
     extern __shared__ __align__(1024) uint8_t sm[];
@@ -402,6 +404,8 @@ __device__ __forceinline__ bool pipe_or256(bool v, int id) {
 
 template <int MODE>
 __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
+    pdl_wait();
+    pdl_launch();
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* img1 = sm + EF_IMG1;
     uint8_t* img2 = sm + EF_IMG2;
@@ -992,6 +996,8 @@ struct ApplyArgs {
 };
 
 __global__ void k_apply(ApplyArgs a) {
+    pdl_wait();
+    pdl_launch();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= a.n[0] + a.n[1]) return;
     const int s = i < a.n[0] ? 0 : 1;
@@ -1019,6 +1025,8 @@ __global__ void k_apply(ApplyArgs a) {
 
 __global__ void k_maxdev(const float* __restrict__ a, const float* __restrict__ b, float ref, int n, float inv,
                          float* __restrict__ out) {
+    pdl_wait();
+    pdl_launch();
     float m = 0.0f;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         m = fmaxf(m, fabsf(a[i] - (b ? b[i] : ref)) * inv);
@@ -1030,6 +1038,8 @@ __global__ void k_maxdev(const float* __restrict__ a, const float* __restrict__ 
 // node inputs and the radius graph
 // ---------------------------------------------------------------------------
 __global__ void k_nodes(sphdem_mpnn_nodes_t a) {
+    pdl_wait();
+    pdl_launch();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int nf = a.n_fluid, nd = a.n_dem, nb = a.n_wall, nw = a.n_dem_wall;
     if (i >= nf + nd + nb + nw) return;
@@ -1082,6 +1092,8 @@ __global__ void k_nodes(sphdem_mpnn_nodes_t a) {
 template <bool FILL>
 __global__ void k_graph(Geo g, const float4* __restrict__ pos, int n_recv, float r2, float rq, int* __restrict__ offset,
                         int* __restrict__ sender, int* __restrict__ receiver, int cap, sphdem_ctl_t* ctl) {
+    pdl_wait();
+    pdl_launch();
     const int i = (int)((blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= n_recv) return;  // warp-uniform
@@ -1165,7 +1177,7 @@ int rows(const uint16_t* A, int M, const uint16_t* B, const float* bias, float* 
     if (rc) return rc;
     const int tiles = (M + kT - 1) / kT;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-    k_rows<K, N, EPI, IMG><<<grid, kT, bytes, st>>>(A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status, list,
+    launch_pdl(k_rows<K, N, EPI, IMG>, grid, kT, bytes, st, A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status, list,
                                                     n_direct);
     return launch_status("mpnn rows");
 }
@@ -1235,7 +1247,7 @@ template <int MODE>
 int edges(const EdgeArgs& a, int grid, cudaStream_t st) {
     int rc = smem_opt_in(k_edges<MODE>, EF_BYTES);
     if (rc) return rc;
-    k_edges<MODE><<<grid, 2 * kPT, EF_BYTES, st>>>(a);
+    launch_pdl(k_edges<MODE>, grid, 2 * kPT, EF_BYTES, st, a);
     return launch_status("mpnn edges");
 }
 
@@ -1268,7 +1280,7 @@ extern "C" int sphdem_mpnn_nodes(const sphdem_mpnn_nodes_t* in, sphdem_stream_t 
     }
     const long n = (long)in->n_fluid + in->n_dem + in->n_wall + in->n_dem_wall;
     if (n <= 0) return SPHDEM_OK;
-    k_nodes<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(*in);
+    launch_pdl(k_nodes, blocks_for(n, 256), 256, 0, as_stream(stream), *in);
     return launch_status("mpnn_nodes");
 }
 
@@ -1297,10 +1309,10 @@ extern "C" int sphdem_mpnn_graph(sphdem_grid_t* grid, const float* node_pos3, co
     const float rq = pad_radius(radius);
     const float4* p4 = reinterpret_cast<const float4*>(node_pos4);
     const int nb = blocks_for((long)n_recv * 32, 256);
-    k_graph<false><<<nb, 256, 0, st>>>(g, p4, n_recv, r2, rq, offset, sender, receiver, edge_capacity, ctl);
+    launch_pdl(k_graph<false>, nb, 256, 0, st, g, p4, n_recv, r2, rq, offset, sender, receiver, edge_capacity, ctl);
     rc = scan_counts(offset, n_recv, scan_scratch, st);
     if (rc) return rc;
-    k_graph<true><<<nb, 256, 0, st>>>(g, p4, n_recv, r2, rq, offset, sender, receiver, edge_capacity, ctl);
+    launch_pdl(k_graph<true>, nb, 256, 0, st, g, p4, n_recv, r2, rq, offset, sender, receiver, edge_capacity, ctl);
     return launch_status("mpnn_graph");
 }
 
@@ -1311,6 +1323,8 @@ namespace {
 // independent).  Edge count from the CSR offsets.
 __global__ void k_mark_senders(const int* __restrict__ offset, const int* __restrict__ sender, int n_recv,
                                int* __restrict__ active, int* __restrict__ list) {
+    pdl_wait();
+    pdl_launch();
     const int E = __ldg(offset + n_recv);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
         const int s = __ldg(sender + e);
@@ -1336,7 +1350,7 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
             set_error("mpnn_forward", e);
             return SPHDEM_ERR_CUDA;
         }
-        k_mark_senders<<<2 * sm_count(), 256, 0, st>>>(n->offset, n->sender, nr, n->active, n->active_list);
+        launch_pdl(k_mark_senders, 2 * sm_count(), 256, 0, st, n->offset, n->sender, nr, n->active, n->active_list);
         list = n->active_list;
     }
     int rc = rows<16, 128, EPI_SILU, true>(n->x, nn, n->packed + P_N1, n->theta + SPHDEM_MPNN_N1_B, nullptr, n->h0,
@@ -1519,7 +1533,7 @@ extern "C" int sphdem_mpnn_apply(float* f_pos, float* f_vel, const float* f_acc,
     a.target = target;
     const int n = n_fluid + n_dem;
     if (n == 0) return SPHDEM_OK;
-    k_apply<<<blocks_for(n, 256), 256, 0, as_stream(stream)>>>(a);
+    launch_pdl(k_apply, blocks_for(n, 256), 256, 0, as_stream(stream), a);
     return launch_status("mpnn_apply");
 }
 
@@ -1532,7 +1546,7 @@ extern "C" int sphdem_mpnn_maxdev(const float* a, const float* b, float ref, int
     if (n == 0) return SPHDEM_OK;
     int grid = blocks_for(n, 256);
     if (grid > 4 * sm_count()) grid = 4 * sm_count();
-    k_maxdev<<<grid, 256, 0, as_stream(stream)>>>(a, b, ref, n, inv, out);
+    launch_pdl(k_maxdev, grid, 256, 0, as_stream(stream), a, b, ref, n, inv, out);
     return launch_status("mpnn_maxdev");
 }
 
