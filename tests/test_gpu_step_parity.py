@@ -256,3 +256,31 @@ def test_fixed_boundary_contact_and_release():
     D.omega.zero_()
     run_bc_dem(D, DB, grids[3], s.dem_bnd_radius, s.dt)
     np.testing.assert_allclose(contact_history(D, "bnd", 0, first_neighbour), first_history, rtol=1e-6, atol=1e-9)
+
+
+def test_c_abi_step_matches_the_graph_replayed_step():
+    """The C entry a non-Python caller binds (sphdem_sphdem_onestep: eager
+    launches on grids built by sphdem_grid_build) and SPHDEM_OneStep (the
+    loop-body CUDA graph) advance identical states identically, bit for bit."""
+    import ctypes as C
+
+    from warp_sph_gpt_gb300 import _lib
+    from warp_sph_gpt_gb300.engine import context_for
+
+    kw = dict(dem_nx=3, dem_ny=2, dem_origin_x=0.1, dem_origin_y=0.1, dem_spacing=0.05, dem_origin_z=0.2)
+    s, P, B, D, DB, grids = scene(**kw)
+    s2, P2, B2, D2, DB2, grids2 = scene(**kw)
+    scales = dem_search_scales(D, DB)
+    for step in range(4):
+        SPHDEM_OneStep(s, P, B, D, DB, *grids, step, scales)
+        ctx = context_for(P2, B2, D2, DB2, tuple(grids2))
+        ctx.set_params(s2, scales)
+        ctx.prepare(rebuild_moving=True, wall_key=(float(C.c_float(s2.support).value), float(C.c_float(s2.h).value)))
+        _lib.check(ctx.lib.sphdem_sphdem_onestep(C.byref(ctx.ctx), C.byref(ctx.params), step, ctx.stream), "onestep")
+        D2._flip("dem")
+        D2._flip("bnd")
+    torch.cuda.synchronize()
+    for a, b in ((P.pos, P2.pos), (P.vel, P2.vel), (P.rho, P2.rho), (P.porosity, P2.porosity), (D.pos, D2.pos),
+                 (D.vel, D2.vel), (D.omega, D2.omega), (D.force, D2.force)):
+        np.testing.assert_array_equal(_np(a), _np(b))
+    np.testing.assert_array_equal(_np(D.contact_dem_id_old), _np(D2.contact_dem_id_old))
