@@ -31,6 +31,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 from pathlib import Path
 
@@ -45,7 +46,7 @@ PROFILE_DIR = ROOT / "profiles"
 
 # Algorithmic bytes per unit of each phase's kernel: every input field read
 # once, every output field written once (FP32).  Units: fluid particles unless
-# stated.  See the design doc (roofline).
+# stated.
 PHASE_BYTES = {
     "force": ("fluid", 36 + 24),          # pos, vel, m, rho, pres in; acc, pgf out
     "density": ("fluid", 20 + 8),         # pos, m, flt in; rho, pres out
@@ -145,7 +146,9 @@ class ClockSampler:
     def __init__(self, gpu_index: int):
         self.proc = None
         self.gpu = gpu_index
-        self.path = ROOT / "gpurun_out" / f"clocks_{os.getpid()}.csv"
+        # raw samples (summarised into the JSON line); SPHDEM_CLOCKS_DIR keeps them elsewhere
+        out = Path(os.environ.get("SPHDEM_CLOCKS_DIR", tempfile.gettempdir()))
+        self.path = out / f"sphdem_clocks_{os.getpid()}_{id(self):x}.csv"
 
     def __enter__(self):
         try:

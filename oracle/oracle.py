@@ -1,7 +1,8 @@
 """ctypes binding of the CPU oracle (oracle/sphdem_oracle.c).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker, and by bench.py's CPU-baseline leg.  The product never imports it.
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() (the
+oracle its step is compared with), and by bench.py's CPU-baseline leg.  The
+product never imports it.
 
 ``HostState`` holds numpy copies of the four particle structs (same field
 layout as include/sphdem.h) plus both sides of each contact CSR, and runs the

@@ -1,9 +1,9 @@
 /*
  * sphdem_oracle.c -- CPU restatement of the reference WCSPH-DEM step.
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: the tests, the smoke
- * check and the CPU-baseline leg of bench.py load it; the product path never
- * does.  It restates, kernel by kernel and in the reference's own expression
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle the GPU results are
+ * compared with: the tests, the smoke test and the CPU-baseline leg of
+ * bench.py load it; the product path never does.  It restates, kernel by kernel and in the reference's own expression
  * order, the Warp kernels of hojin9908/Warp_SPH_GPT (the kernel/ directory) and the step
  * ordering of source/Simulation.py.  Each function cites the lines it follows.
  *

@@ -5,8 +5,8 @@
 * ``oracle/_build/liboracle_{f32,f64}.so`` -- the CPU oracle (test
   infrastructure; built here so that one call prepares a fresh machine).
 
-Outputs stay inside the repository (git-ignored) so the GPU machine, which receives
-the sources and rebuilds them, loads exactly these files.
+Outputs stay inside the repository (git-ignored), so a machine that receives
+the sources and rebuilds them loads exactly these files.
 """
 from __future__ import annotations
 
