@@ -403,4 +403,23 @@ inline void launch_pdl(void (*kernel)(P...), dim3 grid, dim3 block, size_t smem,
     cfg.numAttrs = 1;
     cudaLaunchKernelEx(&cfg, kernel, static_cast<P>(args)...);  // errors surface through launch_status
 }
+namespace {
+// Zero fill as a kernel (not a memset node), so it stays in a chain of
+// programmatic dependent launches.
+__global__ void k_zero_words(int* __restrict__ p, long n) {
+    pdl_wait();
+    pdl_launch();
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) p[i] = 0;
+}
+}  // namespace
+
+// Zero `words` 32-bit words at p on st (launch errors surface through the
+// caller's launch_status / cudaGetLastError).
+inline cudaError_t zero_words(void* p, long words, cudaStream_t st) {
+    if (words <= 0) return cudaSuccess;
+    const int grid = blocks_for(words, 256) < 1024 ? blocks_for(words, 256) : 1024;
+    launch_pdl(k_zero_words, grid, 256, 0, st, static_cast<int*>(p), words);
+    return cudaGetLastError();
+}
+
 }  // namespace sd

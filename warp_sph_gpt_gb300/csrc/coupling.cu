@@ -606,7 +606,7 @@ int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, f
     CplArgs a = make_args(c, support, h);
     a.eps_min = eps_min;
     a.eps_max = eps_max;
-    cudaError_t e = cudaMemsetAsync(&c->ctl->n_near, 0, 2 * sizeof(int), st);  // n_near, near_next
+    cudaError_t e = zero_words(&c->ctl->n_near, 2, st);  // n_near, near_next
     if (e != cudaSuccess) {
         set_error("porosity memset", e);
         return SPHDEM_ERR_CUDA;

@@ -297,8 +297,8 @@ int build_grid(sphdem_grid_t* g, const float* pos, sphdem_ctl_t* ctl, cudaStream
                                                g->cursor, g->order, ctl);
         return launch_status("build_grid");
     }
-    cudaError_t e1 = cudaMemsetAsync(g->cell_start, 0, sizeof(int) * (size_t)(ncell + 1), st);
-    cudaError_t e2 = cudaMemsetAsync(g->cursor, 0, sizeof(int) * (size_t)ncell, st);
+    cudaError_t e1 = zero_words(g->cell_start, (long)ncell + 1, st);
+    cudaError_t e2 = zero_words(g->cursor, (long)ncell, st);
     if (e1 != cudaSuccess || e2 != cudaSuccess) {
         set_error("grid memset", e1 != cudaSuccess ? e1 : e2);
         return SPHDEM_ERR_CUDA;

@@ -1344,8 +1344,8 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
     // inference: node layers on the receivers and the other nodes that send
     const int* list = nullptr;
     if (!store_pre && n->active && n->active_list && nn > nr) {
-        cudaError_t e = cudaMemsetAsync(n->active, 0, sizeof(int) * (size_t)nn, st);
-        if (e == cudaSuccess) e = cudaMemsetAsync(n->active_list, 0, sizeof(int), st);
+        cudaError_t e = zero_words(n->active, nn, st);
+        if (e == cudaSuccess) e = zero_words(n->active_list, 1, st);
         if (e != cudaSuccess) {
             set_error("mpnn_forward", e);
             return SPHDEM_ERR_CUDA;
@@ -1359,7 +1359,7 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
     EdgeArgs a = edge_args(n);
     const int eg = edge_grid(n, 1);
     for (int round = 0; round < 2; ++round) {
-        cudaError_t e = cudaMemsetAsync(n->agg, 0, sizeof(float) * (size_t)nr * kH, st);
+        cudaError_t e = zero_words(n->agg, (long)nr * kH, st);
         if (e != cudaSuccess) {
             set_error("mpnn_forward", e);
             return SPHDEM_ERR_CUDA;

@@ -587,7 +587,7 @@ int jump_body(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j,
     TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
     TRY(gather_fluid(c, st));
     TRY(run_density(c, p->support, p->h, false, true, false, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
-    cudaError_t e = cudaMemsetAsync(j->dev, 0, sizeof(float), st);
+    cudaError_t e = zero_words(j->dev, 1, st);
     if (e != cudaSuccess) {
         set_error("jump", e);
         return SPHDEM_ERR_CUDA;
