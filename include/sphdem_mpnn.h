@@ -224,7 +224,7 @@ int sphdem_jump_undo(sphdem_ctx_t* ctx, const sphdem_jump_t* j, sphdem_stream_t 
  * bits), 1 if the last jump fell back.  Every jump runs 1 plain step (plus m
  * for a fallback): the DEM CSR parity flips that many times.  flags as for
  * sphdem_jump.  Needs one eager sphdem_jump on the context first (kernel
- * attributes are set there). */
+ * attributes are set there); 1 <= substeps <= 29. */
 int sphdem_rollout(sphdem_ctx_t* ctx, const sphdem_params_t* p, const sphdem_jump_t* j, int first_step,
                    int n_jumps, float tol, int32_t flags, int32_t* stats, sphdem_stream_t stream);
 

@@ -790,8 +790,8 @@ int capture_rollout(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump
 int sphdem_rollout(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, int first_step, int n_jumps,
                    float tol, int32_t flags, int32_t* stats, sphdem_stream_t stream) {
     if (!valid_ctx(c) || !p || !j || !j->keep || !j->dev || !j->graph_ctl || !j->scan_scratch || j->substeps < 1 ||
-        !stats || n_jumps < 0) {
-        set_error_msg("rollout: invalid arguments");
+        j->substeps > 29 || !stats || n_jumps < 0) {  // graphs keyed by the Shepard pattern of the K steps
+        set_error_msg("rollout: invalid arguments (1 <= substeps <= 29)");
         return SPHDEM_ERR_INVALID;
     }
     cudaStream_t st = as_stream(stream);
