@@ -67,3 +67,36 @@ def test_autotune_picks_fastest_and_caches(tmp_path):
     import json
 
     assert set(json.loads(path.read_text())) == {"case-A", "case-B"}
+
+
+def test_neighbour_capacity():
+    """The density -> force list capacity: 1.25 x a full support ball + 8,
+    a multiple of 8; an explicit request wins; too large a buffer means none."""
+    import math
+
+    from warp_sph_gpt_gb300.engine import NBR_BYTES_MAX, neighbour_capacity
+
+    dx = 0.005
+    cap = neighbour_capacity(792_000, 2.6 * dx, dx ** 3)
+    ball = 4.0 / 3.0 * math.pi * 2.6 ** 3  # 73.6 particles
+    assert cap % 8 == 0 and 1.25 * ball + 8 <= cap < 1.25 * ball + 16
+    assert neighbour_capacity(1000, 2.6 * dx, dx ** 3, request=16) == 16
+    assert neighbour_capacity(1000, 2.6 * dx, dx ** 3, request=0) == 0
+    n_big = NBR_BYTES_MAX // (4 * (2 * cap + 2)) + 1
+    assert neighbour_capacity(n_big, 2.6 * dx, dx ** 3) == 0
+
+
+def test_rollout_accounting():
+    """Host bookkeeping of a device-judged chunk: steps, the largest accepted
+    judge value from its float bits, kernel counts, and the CSR parity."""
+    import numpy as np
+
+    from warp_sph_gpt_gb300.surrogate import rollout_accounting
+
+    stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0, jump_kernels=0)
+    bits = int(np.array(0.0075, np.float32).view(np.int32))
+    odd = rollout_accounting(stats, [50, 2, bits, 0], 9, 2000, 400)
+    assert stats == dict(jumps=50, fallbacks=2, plain_steps=68, learned_steps=432,
+                         max_dev_accepted=float(np.float32(0.0075)), jump_kernels=2000 + 16)
+    assert odd is False  # 68 plain steps
+    assert rollout_accounting(stats, [3, 0, 0, 0], 9, -1, -1) is True and stats["plain_steps"] == 71

@@ -19,6 +19,18 @@ from .grid import HashGrid, empty_grid
 from .struct import BNDptl, DEMBNDptl, DEMptl, SPHptl
 
 KIND_SPH, KIND_BND, KIND_DEM, KIND_DEMBND = 0, 1, 2, 3
+NBR_BYTES_MAX = 16 << 30  # neighbour lists above this size are not kept (the passes walk cells)
+
+
+def neighbour_capacity(n: int, support: float, mean_volume: float, request: int = -1) -> int:
+    """Per-particle capacity of the density -> force neighbour lists: by
+    default 1.25 x the particles a full support ball holds at the mean
+    particle volume, + 8, rounded up to a multiple of 8; ``request`` >= 0 sets
+    it (0 = no lists).  0 when (2 cap + 2) n words exceed NBR_BYTES_MAX."""
+    cap = max(0, int(request))
+    if request < 0 and mean_volume > 0.0:
+        cap = 8 * math.ceil((1.25 * 4.0 / 3.0 * math.pi * support ** 3 / mean_volume + 8.0) / 8.0)
+    return 0 if (2 * cap + 2) * n * 4 > NBR_BYTES_MAX else cap
 
 
 def _require_cuda(t: torch.Tensor, name: str) -> None:
@@ -69,25 +81,16 @@ class StepContext:
             dem_count=torch.zeros(2 * (nd + 1), **i), dem_aux=torch.zeros((nd, 4), **f),
             f_posq=torch.zeros((ns, 4), **f), nbr=torch.zeros(1, **i))
 
-    NBR_BYTES_MAX = 16 << 30
-
     def _neighbour_lists(self, solv, request: int = -1) -> int:
-        """Capacity of the density -> force neighbour lists: by default 1.25 x
-        the fluid particles a full support ball holds (from the mean particle
-        volume m / rho0) + 8; ``request`` >= 0 sets it (0 = no lists).  The
-        buffer is allocated once per (support, rho0, request).  Particles with
-        more members walk their cells (same results)."""
+        """Neighbour-list capacity (neighbour_capacity, mean particle volume
+        m / rho0) and buffer, allocated once per (support, rho0, request).
+        Particles with more members walk their cells (same results)."""
         P = self.sets[0]
         key = (float(solv.support), float(solv.rho0), int(request))
         if P.n == 0 or key == self._nbr_key:
             return self._nbr_cap
-        cap = max(0, int(request))
-        if request < 0:
-            vol = float(P.m.double().mean().item()) / key[1]  # one host sync per key
-            if vol > 0.0:
-                cap = 8 * math.ceil((1.25 * 4.0 / 3.0 * math.pi * key[0] ** 3 / vol + 8.0) / 8.0)
-        if (2 * cap + 2) * P.n * 4 > self.NBR_BYTES_MAX:
-            cap = 0
+        vol = float(P.m.double().mean().item()) / key[1] if request < 0 else 0.0  # one host sync per key
+        cap = neighbour_capacity(P.n, key[0], vol, request)
         self.work["nbr"] = (torch.zeros((2 * cap + 2) * P.n, dtype=torch.int32, device=self.device) if cap
                             else torch.zeros(1, dtype=torch.int32, device=self.device))
         self._nbr_key, self._nbr_cap = key, cap

@@ -625,6 +625,24 @@ def train(net: Network, ts: TrainingSet, members, iters: int, lr: float = 1e-3, 
 # ---------------------------------------------------------------------------
 # rollout: plain step + learned jump + density judge
 # ---------------------------------------------------------------------------
+def rollout_accounting(stats: dict, counts, m: int, k_jump: int, k_body: int) -> bool:
+    """Add one device-judged chunk to ``stats``.  counts = sphdem_rollout's
+    device counters [jumps, fallbacks, largest accepted judge value (float
+    bits), last fell back]; every jump ran 1 plain step and every fallback m
+    more; k_jump / k_body = kernel nodes of the chunk's jump graphs and of
+    their fallback bodies (-1: not captured).  Returns whether the number of
+    plain steps is odd (each swaps the DEM contact CSR sides once)."""
+    jumps, fb, maxbits = int(counts[0]), int(counts[1]), int(counts[2])
+    plain = jumps + m * fb
+    stats["jumps"] += jumps
+    stats["fallbacks"] += fb
+    stats["plain_steps"] += plain
+    stats["learned_steps"] += m * (jumps - fb)
+    stats["max_dev_accepted"] = max(stats["max_dev_accepted"], float(np.array(maxbits, np.int32).view(np.float32)))
+    stats["jump_kernels"] += max(k_jump, 0) + (max(k_body, 0) * fb) // max(jumps, 1)
+    return plain % 2 == 1
+
+
 class LearnedRollout:
     """Advance a case with jumps of K = m + 1 steps (one plain, m learned).
 
@@ -716,17 +734,11 @@ class LearnedRollout:
             self.host[1:2].copy_(self.g.ctl[3:4], non_blocking=True)
             self.host[2:3].copy_(ctx.ctl[3:4], non_blocking=True)
             torch.cuda.current_stream(self.net.device).synchronize()
-            jumps, fb, maxbits, last = (int(v) for v in self.hstats.tolist())
-            if (n + m * fb) % 2:  # each plain step swapped both contact CSRs
+            counts = [int(v) for v in self.hstats.tolist()]
+            if rollout_accounting(self.stats, counts, m, k_jump, k_body):  # odd plain steps: CSR sides swapped
                 D._flip("dem")
                 D._flip("bnd")
-            s = self.stats
-            s["jumps"] += jumps
-            s["fallbacks"] += fb
-            s["plain_steps"] += jumps + m * fb
-            s["learned_steps"] += m * (jumps - fb)
-            s["max_dev_accepted"] = max(s["max_dev_accepted"], float(np.array(maxbits, np.int32).view(np.float32)))
-            s["jump_kernels"] += max(k_jump, 0) + (max(k_body, 0) * fb) // max(n, 1)
+            last = counts[3]
             gflags, cflags = int(self.host[1]), int(self.host[2])
             if cflags:
                 ctx._raise_for(cflags)
