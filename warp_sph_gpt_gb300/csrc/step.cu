@@ -426,6 +426,21 @@ bool valid_ctx(const sphdem_ctx_t* c) {
 }  // namespace
 namespace {
 
+// The jump's backup (or its restore) in one launch: five contiguous segments.
+struct KeepArgs {
+    float* dst[5];
+    const float* src[5];
+    long len[5];
+};
+__global__ void k_keep(KeepArgs a) {
+    pdl_wait();
+    pdl_launch();
+    const long stride = (long)gridDim.x * blockDim.x;
+#pragma unroll 1
+    for (int s = 0; s < 5; ++s)
+        for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < a.len[s]; i += stride) a.dst[s][i] = a.src[s][i];
+}
+
 // stats: [0] jumps, [1] fallbacks, [2] largest accepted judge value (float
 // bits; values are >= 0), [3] 1 if the last jump fell back.  One thread.
 __global__ void k_decide(const float* __restrict__ dev, const sphdem_ctl_t* __restrict__ gctl, float tol,
@@ -551,26 +566,24 @@ int sphdem_run(sphdem_ctx_t* c, const sphdem_params_t* p, int first_step, int n_
 // ---------------------------------------------------------------------------
 namespace {
 
-int copy_d2d(float* dst, const float* src, size_t n, cudaStream_t st) {
-    if (n == 0) return SPHDEM_OK;
-    cudaError_t e = cudaMemcpyAsync(dst, src, n * sizeof(float), cudaMemcpyDeviceToDevice, st);
-    if (e != cudaSuccess) {
-        set_error("jump copy", e);
-        return SPHDEM_ERR_CUDA;
-    }
-    return SPHDEM_OK;
-}
-
 int jump_keep(sphdem_ctx_t* c, const sphdem_jump_t* j, bool restore, cudaStream_t st) {
-    const size_t nf = (size_t)c->sph.n, nd = (size_t)c->dem.n;
+    const long nf = c->sph.n, nd = c->dem.n;
     float* k = j->keep;
     float* live[5] = {c->sph.pos, c->sph.vel, c->dem.pos, c->dem.vel, c->sph.rho};
-    const size_t len[5] = {3 * nf, 3 * nf, 3 * nd, 3 * nd, nf};
+    const long len[5] = {3 * nf, 3 * nf, 3 * nd, 3 * nd, nf};
+    KeepArgs a;
+    long total = 0;
     for (int i = 0; i < 5; ++i) {
-        TRY(restore ? copy_d2d(live[i], k, len[i], st) : copy_d2d(k, live[i], len[i], st));
+        a.dst[i] = restore ? live[i] : k;
+        a.src[i] = restore ? k : live[i];
+        a.len[i] = len[i];
         k += len[i];
+        total += len[i];
     }
-    return SPHDEM_OK;
+    if (total == 0) return SPHDEM_OK;
+    const int grid = blocks_for(total / 5 + 1, 256) < 1024 ? blocks_for(total / 5 + 1, 256) : 1024;
+    launch_pdl(k_keep, grid, 256, 0, st, a);
+    return launch_status("jump keep");
 }
 
 int jump_body(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, bool shep, bool fresh,
