@@ -15,7 +15,8 @@
 * A jump after an accepted one reuses the fluid grid its judge built: that
   grid is exactly the re-bin of the current positions.
 * Jumps judged on the device (conditional graph node) that all fall back
-  reproduce the plain method bit for bit.
+  reproduce the plain method bit for bit; an edge-buffer overflow falls back
+  on the device and the host grows the buffer.
 """
 import numpy as np
 import pytest
@@ -143,3 +144,28 @@ def test_device_judged_fallbacks_reproduce_the_plain_method(trained):
         np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
     np.testing.assert_array_equal(plain.D.contact_dem_offset_old.cpu().numpy(),
                                   case.D.contact_dem_offset_old.cpu().numpy())
+
+
+def test_device_judged_rollout_recovers_from_an_edge_capacity_overflow(trained):
+    """A graph that outgrows its edge buffer flags it; the device judge then
+    falls back (the plain method runs those steps), and the host grows the
+    buffer from the graph's own edge count and re-captures: later jumps are
+    accepted again and the accounting stays whole."""
+    from warp_sph_gpt_gb300.batch import Case
+    from warp_sph_gpt_gb300.generate import config_small
+    from warp_sph_gpt_gb300.surrogate import LearnedRollout
+
+    case = Case(config_small())
+    ro = LearnedRollout(case, trained["net"])
+    ro.run(0, 10)  # the host-judged first jump
+    ro.g._alloc_edges(2000)  # far below the ~400k edges of the config-1 graph
+    ro.jump.net = ro.g._net(ro.net)
+    fb0 = ro.stats["fallbacks"]
+    ro.run(10, 60)
+    assert ro.stats["fallbacks"] - fb0 == 6  # every jump of the overflowing chunk fell back
+    assert ro.g.capacity >= ro.g.n_edges()
+    stats = ro.run(70, 100)
+    torch.cuda.synchronize()
+    assert stats["jumps"] - stats["fallbacks"] >= 5  # accepted again
+    assert stats["plain_steps"] + stats["learned_steps"] == 170
+    assert torch.isfinite(case.P.pos).all() and int(ro.g.status()) == 0

@@ -1320,15 +1320,16 @@ namespace sd {
 namespace {
 // Non-receiver senders of the current graph, each listed once: list[0] is
 // their count, list[1 ..] the nodes (order immaterial: node rows are
-// independent).  Edge count from the CSR offsets.
+// independent).  Edge count from the CSR offsets, bounded by the edge buffer
+// (an overflowing graph keeps its full count there but only `cap` edges).
 __global__ void k_mark_senders(const int* __restrict__ offset, const int* __restrict__ sender, int n_recv,
-                               int* __restrict__ active, int* __restrict__ list) {
+                               int n_nodes, int cap, int* __restrict__ active, int* __restrict__ list) {
     pdl_wait();
     pdl_launch();
-    const int E = __ldg(offset + n_recv);
+    const int E = min(__ldg(offset + n_recv), cap);
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
         const int s = __ldg(sender + e);
-        if (s >= n_recv && atomicExch(active + s, 1) == 0) list[1 + atomicAdd(list, 1)] = s;
+        if (s >= n_recv && s < n_nodes && atomicExch(active + s, 1) == 0) list[1 + atomicAdd(list, 1)] = s;
     }
 }
 }  // namespace
@@ -1350,7 +1351,8 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
             set_error("mpnn_forward", e);
             return SPHDEM_ERR_CUDA;
         }
-        launch_pdl(k_mark_senders, 2 * sm_count(), 256, 0, st, n->offset, n->sender, nr, n->active, n->active_list);
+        launch_pdl(k_mark_senders, 2 * sm_count(), 256, 0, st, n->offset, n->sender, nr, nn, n->edge_capacity,
+                   n->active, n->active_list);
         list = n->active_list;
     }
     int rc = rows<16, 128, EPI_SILU, true>(n->x, nn, n->packed + P_N1, n->theta + SPHDEM_MPNN_N1_B, nullptr, n->h0,

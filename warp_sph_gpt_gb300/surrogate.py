@@ -744,7 +744,7 @@ class LearnedRollout:
                 ctx._raise_for(cflags)
             if gflags & 0x8:  # edge capacity: those jumps fell back; grow and re-capture
                 self.g.ctl[3] = 0
-                self.g._alloc_edges(int(self.g.capacity * 1.5))
+                self.g._alloc_edges(self._grown_capacity())
                 self._setup()
             elif gflags:
                 raise RuntimeError(f"learned jump raised device status 0x{gflags:x}")
@@ -800,7 +800,7 @@ class LearnedRollout:
                 ctx._raise_for(cflags)
             if gflags & 0x8:  # edge capacity: grow, re-capture, run this jump's substeps plain
                 self.g.ctl[3] = 0
-                self.g._alloc_edges(int(self.g.capacity * 1.5))
+                self.g._alloc_edges(self._grown_capacity())
                 self.jump = None
                 self._kernels = {}
             elif gflags:
@@ -820,6 +820,13 @@ class LearnedRollout:
                 self.stats["plain_steps"] += m
             step += K
         return fresh
+
+    def _grown_capacity(self) -> int:
+        """Edge capacity after an overflow: the last graph's full edge count
+        (its counting pass completes even when the fill overflows) + 25%, and
+        at least 1.5x the old capacity."""
+        need = int(self.g.buf["offset"][self.g.n_recv].item())
+        return max(int(need * 1.25) + 1024, int(self.g.capacity * 1.5))
 
     def _rebuild_jump(self):
         self._setup()
