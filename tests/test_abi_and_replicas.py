@@ -55,6 +55,10 @@ def test_invalid_calls_return_status_without_a_gpu(lib):
     assert lib.sphdem_sph_onestep(None, None, 0, 1, None) == 2
     assert b"null context" in lib.sphdem_last_error()
     assert lib.sphdem_neighbour_digest(None, 3, 1.0, None, None, None) == 2
+    # the learned jump and the device-judged rollout validate before touching the GPU
+    assert lib.sphdem_jump(None, None, None, 0, 0, None) == 2
+    assert lib.sphdem_rollout(None, None, None, 0, 1, 0.01, 0, None, None) == 2
+    assert lib.sphdem_rollout_kernels(None, 0, 1, 0, 0) == -1
 
 
 def _free_port():
