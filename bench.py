@@ -589,6 +589,7 @@ def learned_arm(args, rank, world, local_rank):
     learned.tune({"lanes_sph": default_lanes(learned.P.n)})
     snapL = learned.snapshot()
     ro = S.LearnedRollout(learned, net)
+    ro.native = not args.rollout_hosted
     ro.run(0, 6 * K)  # both Shepard variants run eagerly once, then are captured
     torch.cuda.synchronize()
     learned.restore(snapL)
@@ -656,6 +657,7 @@ def learned_arm(args, rank, world, local_rank):
                                "(12,500 fluid, 20 DEM, dt=1e-4)", "K": K, "judge_tol": cfg.tol, "judge": cfg.judge,
                    "graph_radius": cfg.radius, "edge_weight": args.edge_weight,
                    "train_noise": [args.noise_x, args.noise_v], "dagger_rounds": args.dagger_rounds, "ema": args.ema,
+                   "rollout": "host-judged" if args.rollout_hosted else "device-judged",
                    "rollout_steps": n, "fluid": learned.P.n, "dem": learned.D.n,
                    "l2": "state < L2 (resident between steps, as in a run)"},
         "plain": {"value": units * n / t_plain, "ms_per_step": t_plain * 1e3 / n, "clocks": clocks_plain.summary()},
@@ -811,6 +813,9 @@ def main():
     ap.add_argument("--rollout-steps", type=int, default=1000, help="learned: steps of the compared rollouts")
     ap.add_argument("--judge-tol", type=float, default=0.01, help="learned: density judge tolerance / rho0")
     ap.add_argument("--ema", type=float, default=0.0, help="learned: parameter moving-average decay (0 = off)")
+    ap.add_argument("--rollout-hosted", action="store_true",
+                    help="learned: judge every jump on the host (one graph launch and read-back per jump) instead "
+                         "of on the device; its kernels are visible to a launch-list profiler")
     ap.add_argument("--dagger-rounds", type=int, default=2,
                     help="learned: rounds of on-policy data (states of judged learned rollouts + plain targets)")
     ap.add_argument("--dagger-cases", type=int, default=16, help="learned: training members rolled out per round")
