@@ -49,25 +49,36 @@ def _noalloc(D, DB, grids, radius_max, bnd_radius_max, g, dt, which):
         D._flip("bnd")
 
 
+def _same_contacts(Dg, Dr):
+    for kind in ("dem", "bnd"):
+        np.testing.assert_array_equal(getattr(Dg, f"contact_{kind}_offset_old").cpu().numpy(),
+                                      getattr(Dr, f"contact_{kind}_offset_old").cpu().numpy())
+        np.testing.assert_array_equal(getattr(Dg, f"contact_{kind}_id_old").cpu().numpy(),
+                                      getattr(Dr, f"contact_{kind}_id_old").cpu().numpy())
+        assert field_err(getattr(Dg, f"tang_{kind}_old").cpu().numpy(),
+                         getattr(Dr, f"tang_{kind}_old").cpu().numpy()) < TOL
+    for name in ("force", "torque"):
+        assert field_err(getattr(Dg, name).cpu().numpy(), getattr(Dr, name).cpu().numpy()) < TOL
+
+
 def test_no_alloc_contacts_match_regular_entry_points():
+    """Separate calls per contact kind (which = 1, then 2) on one copy and the
+    fused call (which = 3: both count passes and both halves of the shared
+    array in one kernel) on a third copy, each against the regular entry
+    points on an identical copy."""
     s, D1, W1, g1 = _case()
     _, D2, W2, g2 = _case()
+    _, D3, W3, g3 = _case()
     scales = dem_search_scales(D1, W1)
     for call in range(2):
         K.force_dem(D1, g1[2], scales[0], s.g, s.dt)
         K.bc_dem(D1, W1, g1[3], scales[1], s.dt)
         _noalloc(D2, W2, g2, scales[0], 0.0, s.g, s.dt, 1)
         _noalloc(D2, W2, g2, 0.0, scales[1], 0.0, s.dt, 2)
+        _noalloc(D3, W3, g3, scales[0], scales[1], s.g, s.dt, 3)
         torch.cuda.synchronize()
-        for kind in ("dem", "bnd"):
-            np.testing.assert_array_equal(getattr(D2, f"contact_{kind}_offset_old").cpu().numpy(),
-                                          getattr(D1, f"contact_{kind}_offset_old").cpu().numpy())
-            np.testing.assert_array_equal(getattr(D2, f"contact_{kind}_id_old").cpu().numpy(),
-                                          getattr(D1, f"contact_{kind}_id_old").cpu().numpy())
-            assert field_err(getattr(D2, f"tang_{kind}_old").cpu().numpy(),
-                             getattr(D1, f"tang_{kind}_old").cpu().numpy()) < TOL
-        for name in ("force", "torque"):
-            assert field_err(getattr(D2, name).cpu().numpy(), getattr(D1, name).cpu().numpy()) < TOL
+        _same_contacts(D2, D1)
+        _same_contacts(D3, D1)
         assert int(D1.contact_dem_offset_old[-1]) > 0 and int(D1.contact_bnd_offset_old[-1]) > 0, call
 
 

@@ -338,8 +338,16 @@ int* g_scratch_ptr[kMaxDevices] = {};
 
 // Device address of the array on the current device, looked up once per
 // device.  In host code the array's name stands for a host-side shadow, not a
-// device address, so it must never be passed to a kernel directly.
-int scratch_for_current_device(int** out) {
+// device address, so it must never be passed to a kernel directly.  The
+// cached address belongs to the device's primary context as it was at the
+// lookup: it does not survive cudaDeviceReset (or any other teardown of that
+// context) in the same process, after which this entry point must not be
+// called on that device again.
+//
+// The array is per device, so the call is refused when the current device is
+// not the one that holds the caller's sphere buffers (the kernel would read
+// one GPU's buffers while counting into another GPU's array).
+int scratch_for_current_device(const void* probe, int** out) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) {
@@ -349,6 +357,19 @@ int scratch_for_current_device(int** out) {
     if (dev < 0 || dev >= kMaxDevices) {
         sd::set_error_msg("contacts (no-alloc): device index beyond the supported range");
         return SPHDEM_ERR_INVALID;
+    }
+    if (probe) {
+        cudaPointerAttributes attr;
+        e = cudaPointerGetAttributes(&attr, probe);
+        if (e != cudaSuccess) {
+            sd::set_error("contacts (no-alloc): cudaPointerGetAttributes", e);
+            return SPHDEM_ERR_CUDA;
+        }
+        if (attr.type == cudaMemoryTypeDevice && attr.device != dev) {
+            sd::set_error_msg("contacts (no-alloc): the sphere buffers live on another GPU than the current "
+                              "device; make their GPU current first");
+            return SPHDEM_ERR_INVALID;
+        }
     }
     std::lock_guard<std::mutex> lock(g_scratch_mu);
     if (!g_scratch_ptr[dev]) {
@@ -381,7 +402,7 @@ extern "C" int sphdem_contacts_noalloc(sphdem_ctx_t* c, float radius_max, float 
         return SPHDEM_ERR_INVALID;
     }
     int* scratch = nullptr;
-    int rc = scratch_for_current_device(&scratch);
+    int rc = scratch_for_current_device(c->dem.n > 0 ? c->dem.pos : nullptr, &scratch);
     if (rc) return rc;
     // Every count entry the rebuild reads is written by its own count pass
     // first, so nothing left in the array by an earlier call is ever used.
