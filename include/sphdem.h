@@ -338,7 +338,10 @@ int sphdem_step_dem(sphdem_ctx_t* c, float dt, sphdem_stream_t s);              
  * return SPHDEM_ERR_INVALID.  Allocates nothing.  The first call on a device
  * looks up the array's device address, so make that first call before any
  * stream capture.  All calls share the one array per device: calls whose GPU
- * work overlaps (different streams) race on it. */
+ * work overlaps (different streams) race on it.  The current device must be
+ * the GPU that holds ctx's sphere buffers (else SPHDEM_ERR_INVALID).  The
+ * looked-up address does not survive cudaDeviceReset in the same process:
+ * after a reset, do not call this entry point on that device again. */
 #define SPHDEM_NOALLOC_MAX_DEM 65536
 int sphdem_contacts_noalloc(sphdem_ctx_t* c, float radius_max, float bnd_radius_max, float g,
                             float dt, int which, sphdem_stream_t s);
@@ -377,6 +380,33 @@ int sphdem_drag_beta(const float* eps, const float* rho, const float* mu,
  * mix64 = the SplitMix64 finaliser.  Device outputs. */
 int sphdem_neighbour_digest(sphdem_ctx_t* c, int relation, float radius,
                             int32_t* count, uint64_t* hash, sphdem_stream_t s);
+/* Member sets the hot-path kernels themselves decided in the last step, per
+ * fluid particle in point order, in the digest form above (count, sum of
+ * mix64(neighbour point index)):
+ *   DENSITY_FLUID / DENSITY_WALL: the members the density pass recorded in
+ *     work.nbr (its d2 < s*s decisions; relations SPH_SPH_SUPPORT and
+ *     SPH_BND_SUPPORT); a particle whose list overflowed is digested by the
+ *     same cell walk the force pass then takes;
+ *   FORCE_FLUID / FORCE_WALL: the members the force pass sums over (the
+ *     recorded lists with 1e-12 < d2, or its own walk when a list overflowed;
+ *     relations SPH_SPH_FORCE and SPH_BND_FORCE);
+ *   POROSITY_NEAR: count = 1 for the particles the porosity pass listed as
+ *     having a DEM within 2 h_b (relation SPH_DEM_2H non-empty), else 0.
+ * Positions are the sorted copies of the step's start (work.f_posm, b_posm);
+ * p supplies the support and the list capacity of the step. */
+#define SPHDEM_MEMBERS_DENSITY_FLUID 0
+#define SPHDEM_MEMBERS_DENSITY_WALL  1
+#define SPHDEM_MEMBERS_FORCE_FLUID   2
+#define SPHDEM_MEMBERS_FORCE_WALL    3
+#define SPHDEM_MEMBERS_POROSITY_NEAR 4
+#define SPHDEM_MEMBERS_COUNT         5
+int sphdem_member_digest(sphdem_ctx_t* c, const sphdem_params_t* p, int which, int32_t* count, uint64_t* hash,
+                         sphdem_stream_t s);
+/* Self-test of the bounded device-side wait (no reference counterpart): one
+ * CTA waits `polls` times (0..2^20) on a shared-memory barrier that nothing
+ * arrives at -- no copy or MMA is issued -- then ORs SPHDEM_FLAG_TIMEOUT into
+ * ctl->status and exits, exactly as a staged kernel whose copy never lands. */
+int sphdem_wait_selftest(sphdem_ctl_t* ctl, int polls, sphdem_stream_t s);
 /* FP64 global diagnostics of fluid + moving DEM: out[0] fluid mass, out[1] DEM
  * mass, out[2..4] momentum, out[5] translational kinetic energy, out[6]
  * rotational kinetic energy, out[7] potential energy m*g*z.  out is a device

@@ -100,3 +100,25 @@ def test_rollout_accounting():
                          max_dev_accepted=float(np.float32(0.0075)), jump_kernels=2000 + 16)
     assert odd is False  # 68 plain steps
     assert rollout_accounting(stats, [3, 0, 0, 0], 9, -1, -1) is True and stats["plain_steps"] == 71
+
+
+def test_domain_box_leaves_out_non_finite_positions():
+    """A NaN or Inf position does not poison the grid box (it bins to a face
+    cell on the device, which flags it); the box spans the finite points."""
+    from types import SimpleNamespace
+
+    from warp_sph_gpt_gb300.engine import StepContext
+    from warp_sph_gpt_gb300.struct import BNDptl, SPHptl
+
+    P, B = SPHptl(3, "cpu"), BNDptl(2, "cpu")
+    P.pos.copy_(torch.tensor([[0.0, 1.0, 2.0], [float("nan"), 5.0, 1.0], [3.0, -1.0, float("inf")]]))
+    B.pos.copy_(torch.tensor([[-1.0, 0.5, 0.0], [0.5, 0.5, 0.5]]))
+    ctx = SimpleNamespace(box=None, sets=[P, B])  # the box logic alone (a context pins host memory)
+    lo, hi = StepContext._domain(ctx)
+    assert lo == [-1.0, 0.5, 0.0]
+    assert hi[:2] == [0.5, 1.0] and hi[2] == pytest.approx(2.0 + 0.5 * 2.0)
+    P.pos.fill_(float("nan"))
+    B.pos.fill_(float("nan"))
+    ctx.box = None
+    lo, hi = StepContext._domain(ctx)
+    assert all(np.isfinite(lo)) and all(np.isfinite(hi))

@@ -124,6 +124,7 @@ FLAG_TIMEOUT = 0x10
 ABI_VERSION = 9
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
+MEMBERS = dict(DENSITY_FLUID=0, DENSITY_WALL=1, FORCE_FLUID=2, FORCE_WALL=3, POROSITY_NEAR=4)
 REL = dict(SPH_SPH_SUPPORT=0, SPH_BND_SUPPORT=1, BND_SPH_SUPPORT=2, BND_BND_SUPPORT=3, SPH_SPH_FORCE=4,
            SPH_BND_FORCE=5, SPH_SPH_LEN=6, SPH_DEM_2H=7, DEM_SPH_2H=8, DEM_DEM_2H=9, SPH_DEM_REACT=10)
 
@@ -160,6 +161,8 @@ _SIGNATURES = {
     "sphdem_drag_beta": ([C.c_void_p] * 5 + [C.c_int32, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_neighbour_digest": ([C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p],
                                 C.c_int),
+    "sphdem_wait_selftest": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "sphdem_member_digest": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_diagnostics": ([C.c_void_p, C.c_float, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_format_f32": ([C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32], C.c_int64),
     "sphdem_format_i32": ([C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32], C.c_int64),

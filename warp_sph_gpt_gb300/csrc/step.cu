@@ -18,6 +18,7 @@
 
 #include "common.cuh"
 #include "sphdem_mpnn.h"
+#include "tma.cuh"
 
 namespace sd {
 
@@ -369,6 +370,84 @@ __global__ void k_digest(DigArgs a) {
     a.hash[i] = hs;
 }
 
+// Member digests of the hot-path kernels' own decisions (not a re-evaluation
+// of the predicate): the density pass's recorded member lists, the members the
+// force pass takes from them (or, for a particle whose lists overflowed, from
+// its own cell walk -- exactly the branch k_force takes), and the porosity
+// pass's near list.  One thread per fluid slot; outputs by point index.
+struct MemArgs {
+    Geo gs, gb;
+    const float4* __restrict__ f_posm;
+    const float4* __restrict__ b_posm;
+    const int* __restrict__ nbr;
+    int cap, n, which;
+    float s2, rq;
+    int32_t* count;
+    uint64_t* hash;
+};
+
+__global__ void k_member_digest(MemArgs a) {
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= a.n) return;
+    const int o = a.gs.order[k];
+    const float4 p = a.f_posm[k];
+    const bool wall = a.which == SPHDEM_MEMBERS_DENSITY_WALL || a.which == SPHDEM_MEMBERS_FORCE_WALL;
+    const bool force = a.which == SPHDEM_MEMBERS_FORCE_FLUID || a.which == SPHDEM_MEMBERS_FORCE_WALL;
+    const size_t n = (size_t)a.n;
+    int cf = 0, cb = 0;
+    bool listed = false;
+    if (a.nbr && a.cap > 0) {
+        cf = a.nbr[(size_t)(2 * a.cap) * n + k];
+        cb = a.nbr[(size_t)(2 * a.cap + 1) * n + k];
+        // the force pass reads both lists only when neither overflowed; the
+        // density pass's record of one kind is complete when it fits
+        listed = force ? (cf <= a.cap && cb <= a.cap) : (wall ? cb <= a.cap : cf <= a.cap);
+    }
+    int cnt = 0;
+    uint64_t hs = 0;
+    const Geo& G = wall ? a.gb : a.gs;
+    const float4* q4 = wall ? a.b_posm : a.f_posm;
+    auto take = [&](int j) {
+        ++cnt;
+        hs += mix64((uint64_t)G.order[j]);
+    };
+    if (listed) {
+        const int c = wall ? cb : cf;
+        const int row0 = wall ? a.cap : 0;
+        for (int t = 0; t < c; ++t) {
+            const int j = a.nbr[(size_t)(row0 + t) * n + k];
+            if (force) {
+                const float4 q = q4[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (!(r.d2 > kR2Min)) continue;
+            }
+            take(j);
+        }
+    } else if (G.ncl > 0) {
+        const int inst = inst_of(a.gs, o);
+        for_each_range_ball(G, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
+            for (int j = s; j < e; ++j) {
+                const float4 q = q4[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 < a.s2 && (!force || r.d2 > kR2Min)) take(j);
+            }
+        });
+    }
+    a.count[o] = cnt;
+    a.hash[o] = hs;
+}
+
+// Near-list membership: count[point] = 1 for every listed fluid slot.
+__global__ void k_near_digest(const int* __restrict__ order, const int* __restrict__ near_list,
+                              const sphdem_ctl_t* __restrict__ ctl, int n, int32_t* count, uint64_t* hash) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nn = ctl->n_near;
+    if (i >= nn || i >= n) return;
+    const int o = order[near_list[i]];
+    count[o] = 1;
+    hash[o] = 0;
+}
+
 // ---------------------------------------------------------------------------
 // FP64 diagnostics (no reference counterpart): one block, fixed order.
 // ---------------------------------------------------------------------------
@@ -406,6 +485,22 @@ __global__ void __launch_bounds__(1024) k_diag(sphdem_sph_t P, sphdem_dem_t D, f
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += red[k][threadIdx.x];
         out[threadIdx.x] = t;
     }
+}
+
+// Self-test of the bounded shared-memory barrier wait every staged kernel
+// uses: a barrier that expects one arrival which never comes (no bulk copy
+// or MMA is issued, so nothing asynchronous can be left in flight), polled
+// `polls` times; on giving up the kernel raises SPHDEM_FLAG_TIMEOUT, as the
+// production kernels do, and returns.
+__global__ void k_wait_selftest(sphdem_ctl_t* ctl, int polls) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    const bool landed = mbar_wait(&bar, 0u, polls);
+    if (__syncthreads_or(!landed) && threadIdx.x == 0) flag(ctl, SPHDEM_FLAG_TIMEOUT);
 }
 
 __global__ void k_wendland(const float* r, int n, Kern k, float* w, float* dw) {
@@ -1029,6 +1124,50 @@ int sphdem_wendland(const float* r, int32_t n, float h, float* w, float* dw, sph
 int sphdem_drag_beta(const float* eps, const float* rho, const float* mu, const float* d, const float* speed,
                      int32_t n, float* out, sphdem_stream_t s) {
     return run_drag_beta(eps, rho, mu, d, speed, n, out, as_stream(s));
+}
+
+int sphdem_wait_selftest(sphdem_ctl_t* ctl, int polls, sphdem_stream_t s) {
+    if (!ctl || polls < 0 || polls > (1 << 20)) {
+        set_error_msg("wait self-test: control block and 0 <= polls <= 2^20 required");
+        return SPHDEM_ERR_INVALID;
+    }
+    k_wait_selftest<<<1, 64, 0, as_stream(s)>>>(ctl, polls);
+    return launch_status("wait self-test");
+}
+
+int sphdem_member_digest(sphdem_ctx_t* c, const sphdem_params_t* p, int which, int32_t* count, uint64_t* hash,
+                         sphdem_stream_t s) {
+    if (!valid_ctx(c) || !p || !count || !hash) return SPHDEM_ERR_INVALID;
+    if (which < 0 || which >= SPHDEM_MEMBERS_COUNT) {
+        set_error_msg("unknown member set");
+        return SPHDEM_ERR_INVALID;
+    }
+    cudaStream_t st = as_stream(s);
+    const int n = c->sph.n;
+    if (n <= 0) return SPHDEM_OK;
+    if (which == SPHDEM_MEMBERS_POROSITY_NEAR) {
+        TRY(zero_words(count, n, st));
+        TRY(zero_words(hash, 2L * n, st));
+        k_near_digest<<<blocks_for(n, 256), 256, 0, st>>>(c->grid_sph.order, c->work.near_list, c->ctl, n, count,
+                                                          hash);
+        return launch_status("near digest");
+    }
+    MemArgs a;
+    a.gs = make_geo(c->grid_sph);
+    a.gb = make_geo(c->grid_bnd);
+    if (c->bnd.n <= 0) a.gb.ncl = 0;
+    a.f_posm = (const float4*)c->work.f_posm;
+    a.b_posm = (const float4*)c->work.b_posm;
+    a.nbr = c->work.nbr;
+    a.cap = (c->work.nbr != nullptr && p->nbr_cap > 0) ? p->nbr_cap : 0;
+    a.n = n;
+    a.which = which;
+    a.s2 = p->support * p->support;
+    a.rq = pad_radius(p->support);
+    a.count = count;
+    a.hash = hash;
+    k_member_digest<<<blocks_for(n, 128), 128, 0, st>>>(a);
+    return launch_status("member digest");
 }
 
 int sphdem_neighbour_digest(sphdem_ctx_t* c, int rel, float radius, int32_t* count, uint64_t* hash,

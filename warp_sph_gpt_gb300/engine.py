@@ -98,20 +98,27 @@ class StepContext:
         return cap
 
     def _domain(self):
-        """Union bounding box of all particle sets (one host sync, once)."""
+        """Union bounding box of all particle sets (one host sync, once).
+        Non-finite positions are left out of the box: they bin to a face cell
+        and the device flags them (SPHDEM_FLAG_NONFINITE -> FloatingPointError
+        at the status check)."""
         if self.box is None:
             los, his = [], []
             for s in self.sets:
                 if s.n > 0:
-                    mn, mx = torch.aminmax(s.pos, dim=0)
-                    los.append(mn)
-                    his.append(mx)
+                    ok = torch.isfinite(s.pos).all(dim=1, keepdim=True)
+                    inf = torch.full_like(s.pos, float("inf"))
+                    los.append(torch.where(ok, s.pos, inf).amin(0))
+                    his.append(torch.where(ok, s.pos, -inf).amax(0))
+            lo_hi = (torch.stack(los).amin(0), torch.stack(his).amax(0)) if los else None
+            if lo_hi is not None and not bool(torch.isfinite(lo_hi[0]).all() & torch.isfinite(lo_hi[1]).all()):
+                los = []  # no finite position at all
             if not los:
                 lo = [0.0, 0.0, 0.0]
                 hi = [1.0, 1.0, 1.0]
             else:
-                lo = torch.stack(los).amin(0).tolist()
-                hi = torch.stack(his).amax(0).tolist()
+                lo = lo_hi[0].tolist()
+                hi = lo_hi[1].tolist()
             # open top: leave room above for splashes (points beyond still bin correctly)
             hi[2] = hi[2] + 0.5 * max(hi[2] - lo[2], 1e-6)
             self.box = (lo, hi)

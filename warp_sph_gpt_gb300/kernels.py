@@ -174,6 +174,22 @@ def neighbour_digest(relation: str, radius: float, P_sph=None, P_bnd=None, P_dem
     return count, hsh
 
 
+def member_digest(which: str, P_sph, P_bnd=None, P_dem=None, P_dem_bnd=None, grids=(None, None, None, None)):
+    """(count, hash) per fluid particle of the member set one hot-path kernel
+    decided in the last step (SPHDEM_MEMBERS_*: the density pass's recorded
+    lists, the force pass's members, the porosity pass's near list).  Reads
+    the step's working copies as they are: call it right after a step with the
+    structs and grids of that step (the same four structs and four grids, so
+    the same context), before anything re-bins them."""
+    ctx = context_for(P_sph, P_bnd, P_dem, P_dem_bnd, grids)  # the step's own context and buffers
+    ctx._fill()
+    count = torch.zeros(P_sph.n, dtype=torch.int32, device=P_sph.device)
+    hsh = torch.zeros(P_sph.n, dtype=torch.int64, device=P_sph.device)
+    _lib.check(ctx.lib.sphdem_member_digest(C.byref(ctx.ctx), C.byref(ctx.params), _lib.MEMBERS[which],
+                                            count.data_ptr(), hsh.data_ptr(), ctx.stream), "member_digest")
+    return count, hsh
+
+
 def diagnostics(P_sph, P_dem=None, g: float = 9.81) -> torch.Tensor:
     """FP64 totals: fluid mass, DEM mass, momentum xyz, translational and
     rotational kinetic energy, potential energy m g z (no reference counterpart)."""

@@ -358,7 +358,10 @@ def _apply(lib, graph: Graph, sets: Sets, net_out, cfg: SurrogateConfig, target_
     d_pos = sets.view("d", "pos") if nd else None
     d_vel = sets.view("d", "vel") if nd else None
     d_acc = sets.view("d", "acc", acc[1] if acc else None) if nd else None
-    scale = C.cast((C.c_float * 4)(*cfg.scale), C.c_void_p)  # host array
+    # host array read by the call itself (not by the kernel): a named local, so
+    # it outlives the call whatever ctypes does with temporaries
+    scale_host = (C.c_float * 4)(*(float(v) for v in cfg.scale))
+    scale = C.c_void_p(C.addressof(scale_host))
     if target_state is None:
         rc = lib.sphdem_mpnn_apply(_p(f_pos), _p(f_vel), _p(f_acc), nf, _p(d_pos), _p(d_vel), _p(d_acc), nd,
                                    _p(net_out), cfg.substeps, cfg.dt, scale, None, None, None, graph.stream())
