@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPHDEM_ABI_VERSION 9
+#define SPHDEM_ABI_VERSION 10
 
 /* ---- return codes ---------------------------------------------------- */
 #define SPHDEM_OK                0
@@ -172,8 +172,10 @@ typedef struct sphdem_ctl {
     int32_t e_dem;      /* directed DEM-DEM contacts of the last rebuild        */
     int32_t e_bnd;      /* directed DEM-wall contacts of the last rebuild       */
     int32_t n_near;     /* fluid particles with a DEM inside its coupling reach */
-    int32_t near_next;  /* next near-list entry to hand out (porosity pass 2)   */
-    int32_t pad[8];
+    int32_t near_next;  /* next near-list entry (or porosity work unit) to hand out */
+    int32_t n_ptiles;   /* subject tiles of the tensor-core porosity pass        */
+    int32_t n_pfb;      /* frame blocks with listed particles (same pass)        */
+    int32_t pad[6];
 } sphdem_ctl_t;
 
 /* Sorted working copies (all device, all [n] in the order of their grid).
@@ -205,6 +207,16 @@ typedef struct sphdem_work {
      * the wall count (a count above cap: that particle walks its cells).
      * cap = params.nbr_cap; NULL or cap 0: no lists. */
     int32_t* nbr;       /* [(2*cap+2), n_sph]                                  */
+    /* scratch of the tensor-core porosity pass (porosity_variant 2); sizes from
+     * sphdem_porosity_scratch.  NULL: that variant is unavailable. */
+    int32_t* pfb;       /* [pfb_words] per frame block listed count, then the list of
+                           frame blocks that have listed particles        */
+    int32_t* ptiles;    /* [4*(n_sph+1)] subject tiles (near start, count, frame block) */
+    float*   ppart;     /* [n_sph*SPHDEM_POROSITY_SLABS] per-slab partial normalisers */
+    int32_t* pflag;     /* [n_sph] listed flag per fluid slot                  */
+    int64_t  pfb_words; /* capacity of pfb in int32 words                      */
+    int32_t  pframe;    /* frame-block edge in fluid cells the scratch is sized for */
+    int32_t  pad_work;
 } sphdem_work_t;
 
 /* Solver controls.  Reference: Solv (input/Config.py:11-49 with the SPH-DEM
@@ -230,7 +242,8 @@ typedef struct sphdem_params {
      * summation order): threads per block of the fluid and wall neighbour
      * loops (64, 128 or 256; 0 = 128), the porosity normaliser implementation
      * (0 = direct loads, one warp per particle; 1 = shared-memory staged with
-     * TMA bulk copies, single-instance grids), and the lanes per subject of
+     * TMA bulk copies, single-instance grids; 2 = pair distances on the tensor
+     * cores, uniform DEM h, needs the work.p* scratch), and the lanes per subject of
      * the density, wall-density and force loops (0/1 = one thread per
      * particle; 32 = one warp per particle, for small systems). */
     int32_t block_sph;
@@ -262,6 +275,16 @@ int64_t     sphdem_scan_scratch(int64_t ncell);
  * dembnd, grid, ctl, work, params, ctx), for bindings to check their mirrors;
  * writes min(n, count) values and returns the count. */
 int         sphdem_struct_sizes(int64_t* out, int n);
+
+/* Work units of the tensor-core porosity pass per subject tile: world-anchored
+ * column slabs, whose partial normalisers are summed in slab order. */
+#define SPHDEM_POROSITY_SLABS 8
+/* Scratch sizes of the tensor-core porosity pass for ctx's fluid grid
+ * geometry (grid_sph set) and a frame-block edge of `frame` cells (the tiles'
+ * centres are the centres of world-anchored blocks of frame^3 cells):
+ * out[0] int32 words of pfb, out[1] int32 words of ptiles, out[2] floats of
+ * ppart, out[3] int32 words of pflag.  Returns 0, or SPHDEM_ERR_INVALID. */
+int sphdem_porosity_scratch(const sphdem_ctx_t* ctx, int frame, int64_t* out);
 
 /* ---- neighbour grid ---------------------------------------------------
  * Replaces wp.HashGrid.build(points, radius) (called at main.py:66,73,85,87).

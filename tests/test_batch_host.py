@@ -122,3 +122,19 @@ def test_domain_box_leaves_out_non_finite_positions():
     ctx.box = None
     lo, hi = StepContext._domain(ctx)
     assert all(np.isfinite(lo)) and all(np.isfinite(hi))
+
+
+def test_porosity_frame_edge():
+    """Frame blocks of the tensor-core porosity pass hold >= 4 tiles of 128 at
+    the mean particle volume, edge 2..8 cells, and depend only on the cell
+    width and the particle volume."""
+    from warp_sph_gpt_gb300.engine import porosity_frame
+
+    dx = 0.005
+    assert porosity_frame(2.6 * dx, dx ** 3) == 4    # cell = support 2h = 2.6 dx: 17.6 particles per cell
+    assert porosity_frame(0.052, 0.02 ** 3) == 4     # config 1
+    assert porosity_frame(1.0, 1e-3) == 2            # 1000 per cell: the minimum edge
+    assert porosity_frame(0.01, 0.01 ** 3) == 8      # one per cell: capped
+    assert porosity_frame(0.0, 1.0) == 4 and porosity_frame(1.0, 0.0) == 4
+    for f in (porosity_frame(c, v) for c in (0.01, 0.013, 0.05) for v in (1e-7, 1e-6, 1e-5)):
+        assert 2 <= f <= 8

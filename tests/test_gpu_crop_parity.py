@@ -204,3 +204,33 @@ def test_porosity_normaliser_at_the_support_boundary():
     assert field_err(got, h64.sph["porosity"]) <= max(FIELD_TOL, 4.0 * field_err(h32.sph["porosity"],
                                                                               h64.sph["porosity"]))
     assert np.abs(got[subjects] - h64.sph["porosity"][subjects]).max() < FIELD_TOL
+
+
+def test_tensor_core_porosity_is_canonical():
+    """The tensor-core normaliser (porosity_variant 2, the default) against the
+    direct one (0) on the large crop: the same porosity within FP32 summation
+    order; a rerun from the same state reproduces it bit for bit; and a
+    different frame-block edge (other tiles, other centres) stays within the
+    same tolerance."""
+    import warp_sph_gpt_gb300.engine as E
+
+    runs = {}
+    for tag, variant, frame in (("mma", 2, None), ("again", 2, None), ("direct", 0, None), ("frame3", 2, 3)):
+        c = _case(config_large_crop, 1)
+        ctx = E.context_for(c.P, c.B, c.D, c.W, tuple(c.grids))
+        ctx.tuning["porosity_variant"] = variant
+        orig = E.porosity_frame
+        if frame is not None:
+            E.porosity_frame = lambda cell, vol: frame
+        try:
+            c.step(0)
+        finally:
+            E.porosity_frame = orig
+        torch.cuda.synchronize()
+        runs[tag] = (_np(c.P.porosity).copy(), int(ctx.ctl[6]))
+    ref, n_near = runs["mma"]
+    assert n_near > 1000
+    np.testing.assert_array_equal(runs["again"][0], ref)
+    assert np.abs(runs["direct"][0] - ref).max() < 2e-6
+    assert np.abs(runs["frame3"][0] - ref).max() < 2e-6
+    assert runs["direct"][1] == n_near == runs["frame3"][1]

@@ -69,10 +69,11 @@ def _compare_csr(D, host):
             assert field_err(tang, ref["tang"]) < 1e-5, f"{kind} tangential history"
 
 
-@pytest.mark.parametrize("origin_z,porosity_variant", [(0.2, 0), (0.60, 0), (0.2, 1)])
+@pytest.mark.parametrize("origin_z,porosity_variant", [(0.2, 0), (0.60, 0), (0.2, 1), (0.2, 2), (0.60, 2)])
 def test_coupled_steps_match_fp64_oracle(origin_z, porosity_variant):
     """Per-step fields against the FP64 oracle, CSR against the FP32 oracle;
-    porosity by the direct (0) and the shared-memory staged (1) normaliser."""
+    porosity by the direct (0), the shared-memory staged (1) and the
+    tensor-core (2) normaliser."""
     from warp_sph_gpt_gb300.engine import context_for
 
     s, P, B, D, DB, grids = scene(dem_nx=3, dem_ny=2, dem_origin_x=0.1, dem_origin_y=0.1, dem_spacing=0.05,

@@ -54,7 +54,7 @@ class GridT(C.Structure):
 
 class CtlT(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("step", "old_dem", "old_bnd", "status", "e_dem", "e_bnd",
-                                         "n_near", "near_next")] + [("pad", C.c_int32 * 8)]
+                                         "n_near", "near_next", "n_ptiles", "n_pfb")] + [("pad", C.c_int32 * 6)]
 
 
 class WorkT(C.Structure):
@@ -62,7 +62,8 @@ class WorkT(C.Structure):
                 ("f_posv", c_float_p), ("f_pgf", c_float_p), ("near_list", c_int_p),
                 ("b_posm", c_float_p), ("b_vel", c_float_p), ("b_rp", c_float_p), ("b_vprev", c_float_p),
                 ("b_self", c_float_p), ("dem_count", c_int_p), ("dem_aux", c_float_p), ("f_posq", c_float_p),
-                ("nbr", c_int_p)]
+                ("nbr", c_int_p), ("pfb", c_int_p), ("ptiles", c_int_p), ("ppart", c_float_p), ("pflag", c_int_p),
+                ("pfb_words", C.c_int64), ("pframe", C.c_int32), ("pad_work", C.c_int32)]
 
 
 class ParamsT(C.Structure):
@@ -121,9 +122,10 @@ FLAG_CSR_DEM_OVERFLOW = 0x1
 FLAG_CSR_BND_OVERFLOW = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_TIMEOUT = 0x10
-ABI_VERSION = 9
+ABI_VERSION = 10
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
+POROSITY_SLABS = 8
 MEMBERS = dict(DENSITY_FLUID=0, DENSITY_WALL=1, FORCE_FLUID=2, FORCE_WALL=3, POROSITY_NEAR=4)
 REL = dict(SPH_SPH_SUPPORT=0, SPH_BND_SUPPORT=1, BND_SPH_SUPPORT=2, BND_BND_SUPPORT=3, SPH_SPH_FORCE=4,
            SPH_BND_FORCE=5, SPH_SPH_LEN=6, SPH_DEM_2H=7, DEM_SPH_2H=8, DEM_DEM_2H=9, SPH_DEM_REACT=10)
@@ -162,6 +164,7 @@ _SIGNATURES = {
     "sphdem_neighbour_digest": ([C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p],
                                 C.c_int),
     "sphdem_wait_selftest": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
+    "sphdem_porosity_scratch": ([C.c_void_p, C.c_int, C.c_void_p], C.c_int),
     "sphdem_member_digest": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_diagnostics": ([C.c_void_p, C.c_float, C.c_void_p, C.c_void_p], C.c_int),
     "sphdem_format_f32": ([C.c_void_p, C.c_int64, C.c_int32, C.c_void_p, C.c_int64, C.c_int32], C.c_int64),

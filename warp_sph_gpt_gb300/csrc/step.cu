@@ -41,6 +41,9 @@ int run_step_dem(const sphdem_ctx_t* c, float dt, cudaStream_t st);
 int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st,
                  int variant = 0);
 int run_interaction_dem(const sphdem_ctx_t* c, float mu, float eps_min, float eps_max, float dt, cudaStream_t st);
+int porosity_setup();
+int porosity_frame_edge(int frame);
+int64_t porosity_frames(const sphdem_grid_t& g, int F);
 int run_react(const sphdem_ctx_t* c, float support, float dt, bool integrate, cudaStream_t st);
 int run_drag_beta(const float* eps, const float* rho, const float* mu, const float* d, const float* speed, int n,
                   float* out, cudaStream_t st);
@@ -579,11 +582,28 @@ int sphdem_struct_sizes(int64_t* out, int n) {
     return m;
 }
 
+int sphdem_porosity_scratch(const sphdem_ctx_t* c, int frame, int64_t* out) {
+    if (!c || !out || frame < 0) {
+        set_error_msg("porosity scratch: null context/output or negative frame edge");
+        return SPHDEM_ERR_INVALID;
+    }
+    const int64_t nfb = porosity_frames(c->grid_sph, porosity_frame_edge(frame));
+    const int64_t n = c->sph.n > 0 ? c->sph.n : 0;
+    out[0] = 2 * (nfb + 1);
+    out[1] = 4 * (n + 1);
+    out[2] = n * SPHDEM_POROSITY_SLABS;
+    out[3] = n;
+    return SPHDEM_OK;
+}
+
 int sphdem_grid_build(sphdem_ctx_t* c, int kind, const sphdem_params_t* p, sphdem_stream_t stream) {
     if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
     cudaStream_t st = as_stream(stream);
     switch (kind) {
         case 0:
+            // kernel attributes of the tensor-core porosity pass, set here --
+            // eagerly, before any graph captures a step that launches it
+            if (c->work.pfb) TRY(porosity_setup());
             TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
             return gather_fluid(c, st);
         case 1:
@@ -1098,7 +1118,8 @@ int sphdem_prep_sphdem(sphdem_ctx_t* c, float support, float h, float sph_suppor
     if (!valid_ctx(c)) return SPHDEM_ERR_INVALID;
     cudaStream_t st = as_stream(s);
     TRY(run_dem_aux(c, st));
-    TRY(run_porosity(c, support, h, eps_min, eps_max, st));
+    // the tensor-core normaliser when the context carries its scratch
+    TRY(run_porosity(c, support, h, eps_min, eps_max, st, c->work.pfb ? 2 : 0));
     sphdem_ctx_t cc = *c;  // -grad p only (mode 2)
     return run_force(&cc, sph_support, sph_h, 0.0f, 0.0f, 2, st);
 }

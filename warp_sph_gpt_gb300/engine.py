@@ -33,6 +33,23 @@ def neighbour_capacity(n: int, support: float, mean_volume: float, request: int 
     return 0 if (2 * cap + 2) * n * 4 > NBR_BYTES_MAX else cap
 
 
+def porosity_frame(cell: float, mean_volume: float) -> int:
+    """Frame-block edge F (in fluid-grid cells) of the tensor-core porosity
+    pass: its subject tiles are the listed particles of world-anchored blocks
+    of F^3 cells, centred on the block.  The smallest F >= 2 whose block holds
+    at least four full tiles of 128 at the mean particle volume (so tiles are
+    mostly full), at most 8 (so |x - centre| stays below ~h).  Depends only on
+    the cell width and the particle volume: every member of a batched state
+    and the same case alone get the same blocks."""
+    if not (cell > 0.0 and mean_volume > 0.0):
+        return 4
+    per_cell = cell ** 3 / mean_volume
+    f = 2
+    while f < 8 and f ** 3 * per_cell < 4 * 128:
+        f += 1
+    return f
+
+
 def _require_cuda(t: torch.Tensor, name: str) -> None:
     if not t.is_cuda:
         raise RuntimeError(f"{name} must be a CUDA tensor: the GB300 step has no CPU path")
@@ -61,9 +78,11 @@ class StepContext:
         self._status_host = torch.zeros(16, dtype=torch.int32, pin_memory=True)
         self._status_event = None
         # launch tuning (results do not depend on it): see autotune.py
-        self.tuning = {"block_sph": 0, "porosity_variant": 0, "lanes_sph": 1, "nbr_cap": -1}
+        self.tuning = {"block_sph": 0, "porosity_variant": 2, "lanes_sph": 1, "nbr_cap": -1}
         self._nbr_key = None
         self._nbr_cap = 0
+        self._mean_vol = 0.0
+        self._pkey = None
         self._alloc_work()
         addr = C.addressof(self.ctx)
         weakref.finalize(self, _release, self.lib, addr)
@@ -89,13 +108,36 @@ class StepContext:
         key = (float(solv.support), float(solv.rho0), int(request))
         if P.n == 0 or key == self._nbr_key:
             return self._nbr_cap
-        vol = float(P.m.double().mean().item()) / key[1] if request < 0 else 0.0  # one host sync per key
-        cap = neighbour_capacity(P.n, key[0], vol, request)
+        vol = float(P.m.double().mean().item()) / key[1]  # one host sync per key
+        self._mean_vol = vol
+        cap = neighbour_capacity(P.n, key[0], vol if request < 0 else 0.0, request)
         self.work["nbr"] = (torch.zeros((2 * cap + 2) * P.n, dtype=torch.int32, device=self.device) if cap
                             else torch.zeros(1, dtype=torch.int32, device=self.device))
         self._nbr_key, self._nbr_cap = key, cap
         self._sig = None  # pointers changed
         return cap
+
+    def _porosity_scratch(self) -> None:
+        """Scratch of the tensor-core porosity pass (work.pfb, ptiles, ppart,
+        pflag), sized by the library for the fluid grid geometry and the frame
+        edge; allocated once per geometry.  Coupled contexts with spheres only."""
+        P, D = self.sets[0], self.sets[2]
+        if P.n == 0 or D.n == 0 or self.grids[0].geometry is None:
+            return
+        frame = porosity_frame(self.grids[0].geometry[2], self._mean_vol)
+        key = (frame, tuple(self.grids[0].geometry[0]), tuple(self.grids[0].geometry[1]), self.grids[0].ninst, P.n)
+        if key != self._pkey:
+            out = (C.c_int64 * 4)()
+            _lib.check(self.lib.sphdem_porosity_scratch(C.byref(self.ctx), frame, out), "porosity scratch")
+            i32 = dict(dtype=torch.int32, device=self.device)
+            self.work.update(pfb=torch.zeros(max(1, out[0]), **i32), ptiles=torch.zeros(max(1, out[1]), **i32),
+                             ppart=torch.zeros(max(1, out[2]), dtype=torch.float32, device=self.device),
+                             pflag=torch.zeros(max(1, out[3]), **i32))
+            self._pwords, self._pframe, self._pkey = int(out[0]), frame, key
+            self._sig = None  # pointers changed
+            self._fill()
+        self.ctx.work.pfb_words = self._pwords
+        self.ctx.work.pframe = self._pframe
 
     def _domain(self):
         """Union bounding box of all particle sets (one host sync, once).
@@ -216,6 +258,7 @@ class StepContext:
         wall_key = (support, h) of the wall self-density cache."""
         self._fill()
         self._fill_grids()
+        self._porosity_scratch()
         sph, bnd, dem, dembnd = self.sets
         st = self.stream
         for kind in (KIND_BND, KIND_DEMBND, KIND_SPH, KIND_DEM):
