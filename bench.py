@@ -19,8 +19,8 @@ GPU (the path does not shard), value = sum over ranks.
 
 ``--impl reference`` times the reference algorithm on the host cores instead:
 the CPU oracle (a restatement of the reference's Warp kernels) with all
-threads, on a bounded sample of every step (every S-th subject particle),
-extrapolated to a full step by a two-point fit t(S) = F + V/S.
+threads; the first timed step runs in full, the others on a bounded sample
+(every S-th subject particle) scaled by the measured full/sample ratio.
 """
 from __future__ import annotations
 
@@ -226,22 +226,24 @@ def reduce_max(value: float, world: int, device=None) -> float:
     return float(t.item())
 
 
-# FP32 instructions per candidate of the porosity normaliser's inner loop
-# (csrc/coupling.cu ball_weight_h + accumulate on the scaled copy: 3 sub,
-# 1 mul + 2 fma for s = q^2, 1 min, 4 fma for the Wendland polynomial, 1 fma
-# into the sum) plus one MUFU square root.
-POROSITY_FP32_OPS_PER_PAIR = 13
+# Square roots per SM per clock of the MUFU pipe (sqrt.approx): the tensor-core
+# porosity pass evaluates one per subject-candidate pair of every 128 x 128 chunk.
+MUFU_SQRT_PER_SM_CLK = 16
 
 
 def porosity_compute_roofline(ctx, D, scales, porosity_ms: float, device):
-    """The porosity normaliser is bound by FP32 issue, not HBM: pairs summed
-    per second against the FP32 lane rate / ops per pair.  Pairs are estimated
-    from an exact count over 256 sampled listed particles."""
+    """The porosity normaliser is bound by the pair evaluations, not HBM: the
+    tensor cores give each pair's squared distance and the MUFU pipe its
+    square root, so pairs per second are compared with 152 SMs x 16 square
+    roots per clock.  'evaluated' counts every pair of the evaluated chunks
+    (the tiles' windows), 'in_ball' the pairs inside the coupling support
+    (exact count around 256 sampled listed particles)."""
     import torch
 
     if D.n == 0 or porosity_ms <= 0 or scales[3] <= 0:
         return None
     n_near = int(ctx.ctl[6].item())
+    chunks = int(ctx.ctl[10].item())
     if n_near <= 0:
         return None
     w = ctx.work
@@ -252,16 +254,18 @@ def porosity_compute_roofline(ctx, D, scales, porosity_ms: float, device):
     support = 2.0 * float(scales[3])
     counts = torch.cat([(torch.cdist(subj[i:i + 32], fluid) < support).sum(1) for i in range(0, len(subj), 32)])
     pairs = float(counts.float().mean().item()) * n_near
+    evaluated = float(chunks) * 128 * 128
     props = torch.cuda.get_device_properties(device)
     peaks = json.loads(PEAKS_FILE.read_text()) if PEAKS_FILE.exists() else {}
     mhz = float(peaks.get("sm_max_mhz", 2070.0))
-    lanes = props.multi_processor_count * 128
-    peak_pairs = lanes * mhz * 1e6 / POROSITY_FP32_OPS_PER_PAIR
-    achieved = pairs / (porosity_ms * 1e-3)
-    return {"bound": "fp32", "kernel": "k_porosity_near", "listed_particles": n_near,
-            "pairs_per_step": pairs, "achieved_pairs_per_s": achieved, "peak_pairs_per_s": peak_pairs,
-            "frac": achieved / peak_pairs, "fp32_ops_per_pair": POROSITY_FP32_OPS_PER_PAIR,
-            "peak_basis": f"{props.multi_processor_count} SMs x 128 FP32 lanes x {mhz:.0f} MHz"}
+    peak = props.multi_processor_count * MUFU_SQRT_PER_SM_CLK * mhz * 1e6
+    secs = porosity_ms * 1e-3
+    return {"bound": "mufu", "kernel": "k_porosity_mma", "listed_particles": n_near,
+            "in_ball_pairs_per_step": pairs, "evaluated_pairs_per_step": evaluated,
+            "achieved_pairs_per_s": evaluated / secs, "in_ball_pairs_per_s": pairs / secs,
+            "peak_pairs_per_s": peak, "frac": evaluated / secs / peak, "in_ball_frac": pairs / secs / peak,
+            "peak_basis": f"{props.multi_processor_count} SMs x {MUFU_SQRT_PER_SM_CLK} square roots per clock x "
+                          f"{mhz:.0f} MHz (one per evaluated pair; the squared distances come from tcgen05 MMAs)"}
 
 
 def output_run(args, solv, P, B, D, W, grids, scales, n_units, first_step):
@@ -751,23 +755,55 @@ def cpu_fit(host, solv, scales, budget_s: float):
     return stride, t1, t2, F + V
 
 
+def cpu_full_step(host, solv, scales, step: int) -> float:
+    """Seconds of one complete oracle step (every subject) on a fresh copy."""
+    return cpu_sample(host, solv, scales, 1, step)
+
+
+def cpu_single_thread(host, solv, scales, stride: int, cores: int, t_full: float):
+    """Single-thread figure: one sampled step on 1 thread and on all cores at
+    the same stride; the full single-thread step is the measured full step
+    scaled by their ratio (the reference's Warp CPU launches are serial)."""
+    from oracle import oracle as O
+
+    O.set_threads(1)
+    t1 = cpu_sample(host, solv, scales, stride, 1)
+    O.set_threads(cores)
+    tm = cpu_sample(host, solv, scales, stride, 1)
+    return t1, tm, t_full * t1 / tm if tm > 0 else float("nan")
+
+
 def cpu_baseline(gen, solv, parts, scales, budget_s):
+    """The FP32 oracle on the host cores: one complete step timed (measured),
+    the two-point stride fit kept as a cross-check (extrapolated), and the
+    single-thread figure (sample ratio)."""
     from oracle import oracle as O
 
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
     O.set_threads(cores)
     host = _oracle_state(parts)
-    stride, t1, t2, full = cpu_fit(host, solv, scales, budget_s)
     n_units = len(host.sph["pos"]) + len(host.dem["pos"])
-    return {"value": n_units / full, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-            "sample": f"CPU oracle (restatement of the reference Warp kernels, FP32) on {cores} threads: one coupled "
-                      f"step on every {stride}-th and every {_prime_at_least(2 * stride)}-th subject particle "
-                      f"({t1:.2f} s, {t2:.2f} s; prime strides, a fresh copy of the state per sample), full step "
-                      f"{full:.2f} s from the fit t(S) = F + V/S"}
+    t_full = cpu_full_step(host, solv, scales, 1)
+    stride, t1, t2, fit = cpu_fit(host, solv, scales, budget_s)
+    s1 = _prime_at_least(4 * stride)
+    st1, stm, t_single = cpu_single_thread(host, solv, scales, s1, cores, t_full)
+    return {"value": n_units / t_full, "unit": "particle-steps/s", "cores": cores, "kind": "port",
+            "measured": {"full_step_s": round(t_full, 3), "steps_timed_in_full": 1, "threads": cores},
+            "extrapolated": {"full_step_s": round(fit, 3), "value": n_units / fit,
+                             "method": f"t(S) = F + V/S from one step on every {stride}-th and every "
+                                       f"{_prime_at_least(2 * stride)}-th subject ({t1:.2f} s, {t2:.2f} s)"},
+            "single_thread": {"value": n_units / t_single, "full_step_s": round(t_single, 2),
+                              "method": f"measured full step x (1-thread / {cores}-thread time of one step on "
+                                        f"every {s1}-th subject: {st1:.2f} s / {stm:.2f} s)"},
+            "sample": f"CPU oracle (restatement of the reference Warp kernels, FP32) on {cores} threads: one "
+                      f"complete coupled step of the workload timed ({t_full:.2f} s, fresh copy of the state)"}
 
 
 def reference_arm(args):
-    """--impl reference: the reference algorithm on the host cores."""
+    """--impl reference: the reference algorithm on the host cores.  The first
+    timed step runs every subject (measured); the others run a bounded sample
+    (every S-th subject) scaled by the measured full/sample ratio, so the
+    whole run stays within a few minutes."""
     from oracle import oracle as O
 
     gen, solv, parts, desc = make_case(args.workload, "cpu")
@@ -778,25 +814,32 @@ def reference_arm(args):
     O.set_threads(cores)
     host = _oracle_state(parts)
     n_units = parts[0].n + parts[2].n
-    stride, t1, t2, full = cpu_fit(host, solv, scales, args.cpu_budget_s)
-    samples = []
-    for s in range(args.warmup + args.steps):
-        t = cpu_sample(host, solv, scales, stride, 1 + s)
-        if s >= args.warmup:
-            samples.append(t)
-    mean_sample = statistics.mean(samples) if samples else t1
-    scale = full / t1 if t1 > 0 else 1.0  # sample -> full step
-    step_s = mean_sample * scale
+    stride, t1, t2, fit = cpu_fit(host, solv, scales, args.cpu_budget_s)
+    for s in range(args.warmup):  # warm-up samples (caches, thread pool)
+        cpu_sample(host, solv, scales, stride, 1 + s)
+    t_full = cpu_full_step(host, solv, scales, 1 + args.warmup)
+    t_sample0 = cpu_sample(host, solv, scales, stride, 1 + args.warmup)
+    scale = t_full / t_sample0 if t_sample0 > 0 else 1.0
+    steps = [t_full]
+    for s in range(1, args.steps):
+        steps.append(cpu_sample(host, solv, scales, stride, 1 + args.warmup + s) * scale)
+    step_s = statistics.mean(steps)
     value = n_units / step_s
+    timing = (f"step 1 of {args.steps} timed in full ({t_full:.2f} s, every subject); steps 2-{args.steps} on "
+              f"every {stride}-th subject, scaled by the measured full/sample ratio {scale:.2f}")
     return {"impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
             "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded generator rules of the reference's input_gen)",
             "config": {"workload": desc, "fluid": parts[0].n, "wall": parts[1].n, "dem": parts[2].n,
                        "dem_wall": parts[3].n},
+            "timing": timing,
             "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": cores, "kind": "port",
-                             "sample": f"every {stride}-th subject per step, scaled by the fit F + V/S "
-                                       f"(full step {full:.2f} s)"},
+                             "measured": {"full_step_s": round(t_full, 3), "steps_timed_in_full": 1},
+                             "extrapolated": {"full_step_s": round(fit, 3),
+                                              "method": f"two-point stride fit (strides {stride}, "
+                                                        f"{_prime_at_least(2 * stride)})"},
+                             "sample": timing},
             "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
@@ -835,7 +878,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--output-step", type=int, default=0,
                     help="also time the run with a VTP frame every N steps (asynchronous writer)")
-    ap.add_argument("--porosity-variant", type=int, default=-1, choices=(-1, 0, 1),
+    ap.add_argument("--porosity-variant", type=int, default=-1, choices=(-1, 0, 1, 2),
                     help="porosity normaliser implementation (-1 = library default)")
     ap.add_argument("--lanes-sph", type=int, default=0, choices=(0, 1, 32),
                     help="threads per particle of the SPH loops (0 = by system size)")

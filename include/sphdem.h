@@ -175,7 +175,8 @@ typedef struct sphdem_ctl {
     int32_t near_next;  /* next near-list entry (or porosity work unit) to hand out */
     int32_t n_ptiles;   /* subject tiles of the tensor-core porosity pass        */
     int32_t n_pfb;      /* frame blocks with listed particles (same pass)        */
-    int32_t pad[6];
+    int32_t n_pchunks;  /* 128 x 128 pair chunks the same pass evaluated          */
+    int32_t pad[5];
 } sphdem_ctl_t;
 
 /* Sorted working copies (all device, all [n] in the order of their grid).

@@ -54,7 +54,7 @@ class GridT(C.Structure):
 
 class CtlT(C.Structure):
     _fields_ = [(n, C.c_int32) for n in ("step", "old_dem", "old_bnd", "status", "e_dem", "e_bnd",
-                                         "n_near", "near_next", "n_ptiles", "n_pfb")] + [("pad", C.c_int32 * 6)]
+                                         "n_near", "near_next", "n_ptiles", "n_pfb", "n_pchunks")] + [("pad", C.c_int32 * 5)]
 
 
 class WorkT(C.Structure):

@@ -488,6 +488,7 @@ __global__ void __launch_bounds__(kPThreads, 2) k_porosity_mma(PorArgs a) {
             if (tid == 0) sh.pre[m] = tot;
             __syncthreads();
             const int nchunks = (tot + kPN - 1) / kPN;
+            if (tid == 0 && nchunks > 0) atomicAdd(&a.ctl->n_pchunks, nchunks);
             const bool crs = nchunks <= kPMaxChunks;  // else each candidate searches all ranges
             if (crs) {
                 for (int c = tid; c < nchunks; c += kPThreads) {
@@ -745,8 +746,9 @@ int run_porosity_mma(const sphdem_ctx_t* c, float support, float h, float eps_mi
     const int span = (int)ceilf(2.0f * a.rq / cell) + F + 3;
     a.Wx = (span + kPSlabs - 2) / (kPSlabs - 1);
     if (a.Wx < 1) a.Wx = 1;
-    // counters: listed particles, work units, tiles, listed frame blocks (control words 6..9)
-    cudaError_t e = zero_words(&c->ctl->n_near, 4, st);
+    // counters: listed particles, work units, tiles, listed frame blocks,
+    // evaluated chunks (control words 6..10)
+    cudaError_t e = zero_words(&c->ctl->n_near, 5, st);
     if (e == cudaSuccess) e = zero_words(a.cnt, nfb, st);
     if (e != cudaSuccess) {
         set_error("porosity memset", e);
