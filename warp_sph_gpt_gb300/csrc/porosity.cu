@@ -41,8 +41,8 @@
 //                frame block's first listed particle puts it on a list.
 //   k_plist      one warp per listed frame block: reserves its segment of the
 //                near list and of the tile table (atomics: segment placement
-//                varies, results do not), writes its listed slots in (column,
-//                slot) order and its tiles of <= 128.
+//                varies, results do not), writes its listed slots by 2 x 2 x 2
+//                cell sub-blocks (so a tile of 128 is compact) and its tiles.
 //   k_porosity_mma  persistent, 2 CTAs per SM: work units (tile, slab);
 //                warps 0-7 epilogue (TMEM lane = subject; warp w reads lane
 //                quarter w mod 4, chunk half w / 4), warp 8 issues the MMAs
@@ -242,7 +242,7 @@ __global__ void __launch_bounds__(256) k_pnear(PorArgs a) {
 }
 
 // ---------------------------------------------------------------------------
-// listed slots of each frame block in (column, slot) order, and its tiles
+// listed slots of each frame block by sub-blocks of 2 x 2 x 2 cells, and its tiles
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_plist(PorArgs a) {
     pdl_wait();
@@ -269,18 +269,22 @@ __global__ void __launch_bounds__(256) k_plist(PorArgs a) {
         frame_cells(a, 1, fy, y0, y1);
         frame_cells(a, 2, fz, z0, z1);
         int pos = n0;
-        for (int cx = x0; cx <= x1; ++cx)
-            for (int cy = y0; cy <= y1; ++cy) {
-                const int base = inst * a.gs.ncl + (cx * a.gs.dim[1] + cy) * a.gs.dim[2];
-                const int s = a.gs.start[base + z0], e = a.gs.start[base + z1 + 1];
-                for (int k0 = s; k0 < e; k0 += 32) {
-                    const int k = k0 + lane;
-                    const bool near = k < e && a.flag[k] != 0;
-                    const unsigned m = __ballot_sync(0xffffffffu, near);
-                    if (near) a.near_list[pos + __popc(m & ((1u << lane) - 1u))] = k;
-                    pos += __popc(m);
-                }
-            }
+        // 2 x 2 x 2-cell sub-blocks in turn, so that consecutive tiles are compact
+        for (int bx = x0; bx <= x1; bx += 2)
+            for (int by = y0; by <= y1; by += 2)
+                for (int bz = z0; bz <= z1; bz += 2)
+                    for (int cx = bx; cx <= min(bx + 1, x1); ++cx)
+                        for (int cy = by; cy <= min(by + 1, y1); ++cy) {
+                            const int base = inst * a.gs.ncl + (cx * a.gs.dim[1] + cy) * a.gs.dim[2];
+                            const int s = a.gs.start[base + bz], e = a.gs.start[base + min(bz + 1, z1) + 1];
+                            for (int k0 = s; k0 < e; k0 += 32) {
+                                const int k = k0 + lane;
+                                const bool near = k < e && a.flag[k] != 0;
+                                const unsigned m = __ballot_sync(0xffffffffu, near);
+                                if (near) a.near_list[pos + __popc(m & ((1u << lane) - 1u))] = k;
+                                pos += __popc(m);
+                            }
+                        }
         for (int t = lane; t < nt; t += 32) a.tiles[t0 + t] = make_int4(n0 + kPM * t, min(kPM, c - kPM * t), fb, 0);
     }
 }
@@ -295,20 +299,23 @@ __device__ __forceinline__ bool bwait(uint64_t* bar, uint32_t parity, PorSmem& s
     return false;
 }
 
-// 16 columns of this thread's TMEM lane, loaded and waited for in one
+// 32 columns of this thread's TMEM lane, loaded and waited for in one
 // statement (the registers are defined only once the data has landed).
-__device__ __forceinline__ void ld16(uint32_t taddr, uint32_t* r) {
+__device__ __forceinline__ void ld32(uint32_t taddr, uint32_t* r) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
         : "r"(taddr)
         : "memory");
 }
 
-// The weighted sums of 16 chunk columns starting at a multiple of 16: column
+// The weighted sums of 32 chunk columns starting at a multiple of 32: column
 // 4i + c holds a candidate of class c (or c + 4 in the second half of the
 // chunk) and goes to accumulator c.  u^4 (1 + 2q), u = 1 - q/2, is evaluated
 // as the expanded polynomial 1 + s (-5/2 + q (5/2 + q (-15/16 + q/8))) with s
@@ -316,17 +323,17 @@ __device__ __forceinline__ void ld16(uint32_t taddr, uint32_t* r) {
 // there is exactly 0.  The polynomial and the sums run on packed FP32 pairs
 // (fma.rn.f32x2: two independent round-to-nearest FMAs, the values of the
 // scalar ones).
-__device__ __forceinline__ void sums16(const uint32_t* r, const float* V, float2& a01, float2& a23) {
+__device__ __forceinline__ void sums32(const uint32_t* r, const float* V, float2& a01, float2& a23) {
     const float2 k0 = make_float2(0.125f, 0.125f), k1 = make_float2(-0.9375f, -0.9375f);
     const float2 k2 = make_float2(2.5f, 2.5f), k3 = make_float2(-2.5f, -2.5f), one = make_float2(1.0f, 1.0f);
     const float4* V4 = reinterpret_cast<const float4*>(V);
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
-        const float4 v = V4[i];
+    for (int i = 0; i < 8; ++i) {
         const float s0 = fminf(fabsf(__uint_as_float(r[4 * i])), 4.0f);
         const float s1 = fminf(fabsf(__uint_as_float(r[4 * i + 1])), 4.0f);
         const float s2 = fminf(fabsf(__uint_as_float(r[4 * i + 2])), 4.0f);
         const float s3 = fminf(fabsf(__uint_as_float(r[4 * i + 3])), 4.0f);
+        const float4 v = V4[i];
         const float2 sa = make_float2(s0, s1), sb = make_float2(s2, s3);
         const float2 qa = make_float2(sqrt_apx(s0), sqrt_apx(s1)), qb = make_float2(sqrt_apx(s2), sqrt_apx(s3));
         const float2 ca = __ffma2_rn(__ffma2_rn(__ffma2_rn(k0, qa, k1), qa, k2), qa, k3);
@@ -580,15 +587,15 @@ __global__ void __launch_bounds__(kPThreads, 2) k_porosity_mma(PorArgs a) {
                         break;
                     }
                     umma::fence_after();
-                    const unsigned act = (warp >> 2) ? 0xf0u : 0x0fu;  // this warp's half: 4 pieces of 16
-                    // the other epilogue warps of the sub-partition hide each load
-                    const uint32_t tcol = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + b * kPN;
+                    // this warp's half of the chunk, 32 columns per load; the
+                    // other epilogue warps of the sub-partition hide each load
+                    const int h0 = (warp >> 2) * (kPN / 2);
+                    const uint32_t tcol = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + b * kPN + h0;
 #pragma unroll 1
-                    for (int kc = 0; kc < 8; ++kc) {
-                        if (!((act >> kc) & 1u)) continue;
-                        uint32_t r[16];
-                        ld16(tcol + 16 * kc, r);
-                        sums16(r, &sh.V[s][16 * kc], acc01, acc23);
+                    for (int kc = 0; kc < kPN / 2; kc += 32) {
+                        uint32_t r[32];
+                        ld32(tcol + kc, r);
+                        sums32(r, &sh.V[s][h0 + kc], acc01, acc23);
                     }
                     umma::fence_before();
                     __syncwarp();
