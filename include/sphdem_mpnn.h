@@ -179,9 +179,12 @@ int sphdem_mpnn_maxdev(const float* a, const float* b, float ref, int32_t n, flo
  *      `substeps` steps applied in place (sphdem_mpnn_apply);
  *   4. the judge: fluid grid rebuilt and the filtered fluid density
  *      evaluated at the new positions (the density pass of the plain step),
- *      *dev = max_i |rho_new - rho_old| / rho0 (judge 0) or
- *      max_i |rho_new - rho0| / rho0 (judge 1).
- * The caller reads *dev (and net.status) and, above its tolerance, calls
+ *      dev[0] = max_i |rho_new - rho_old| / rho0 (judge 0) or
+ *      max_i |rho_new - rho0| / rho0 (judge 1); and the position term
+ *      dev[1] = max_i |s_x out_x,i| + m dt |s_v out_v,i|, how far the
+ *      network's correction moves a particle beyond the constant-acceleration
+ *      prior, or will have moved it one jump later through its velocity [m].
+ * The caller reads dev (and net.status) and, above its tolerances, calls
  * sphdem_jump_undo and runs the substeps with sphdem_run.  The plain step of
  * 1. flips the DEM contact CSR parity once. */
 typedef struct sphdem_jump {
@@ -194,10 +197,12 @@ typedef struct sphdem_jump {
     int32_t substeps;
     float scale[4];             /* output scales, as sphdem_mpnn_apply's scale4 */
     float* keep;                /* [6 n_fluid + 6 n_dem + n_fluid] backup */
-    float* dev;                 /* [1] judge result (device) */
+    float* dev;                 /* [2] judge values (device): [0] the density term below,
+                                   [1] the largest correction displacement: max over
+                                   particles of |s_x out_x| + m dt |s_v out_v| [m] */
     int32_t judge;              /* 0: max |rho_new - rho_old| / rho0 (change over the jump);
                                    1: max |rho_new - rho0| / rho0 (density deviation) */
-    int32_t pad_jump;
+    float pos_tol;              /* > 0: a jump whose dev[1] exceeds it [m] falls back too */
 } sphdem_jump_t;
 
 /* flags bit 0 (SPHDEM_JUMP_GRID_FRESH): the fluid grid is current -- the last
@@ -216,12 +221,14 @@ int sphdem_jump_kernels(sphdem_ctx_t* ctx, int variant);
 int sphdem_jump_undo(sphdem_ctx_t* ctx, const sphdem_jump_t* j, sphdem_stream_t stream);
 
 /* n_jumps jumps from first_step, judged on the device: each is the jump's
- * graph plus a judge that, when *j->dev > tol (or a graph/kernel flag is
+ * graph plus a judge that, when j->dev[0] > tol, or j->pos_tol > 0 and
+ * j->dev[1] > j->pos_tol (or a graph/kernel flag is
  * set), runs the fallback in a conditional graph node -- undo, the m
  * substeps as plain steps, a fluid re-bin -- so the host launches the jumps
- * back to back and reads the outcome once.  stats (device int32[4], the
- * caller zeroes it): jumps, fallbacks, largest accepted judge value (float
- * bits), 1 if the last jump fell back.  Every jump runs 1 plain step (plus m
+ * back to back and reads the outcome once.  stats (device int32[6], the
+ * caller zeroes it): jumps, fallbacks, largest accepted density judge value
+ * (float bits), 1 if the last jump fell back, largest accepted position term
+ * (float bits), unused.  Every jump runs 1 plain step (plus m
  * for a fallback): the DEM CSR parity flips that many times.  flags as for
  * sphdem_jump.  Needs one eager sphdem_jump on the context first (kernel
  * attributes are set there); 1 <= substeps <= 29. */

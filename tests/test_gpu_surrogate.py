@@ -146,6 +146,38 @@ def test_device_judged_fallbacks_reproduce_the_plain_method(trained):
                                   case.D.contact_dem_offset_old.cpu().numpy())
 
 
+@pytest.mark.parametrize("native", [True, False])
+def test_position_judge_alone_forces_the_plain_method(trained, native):
+    """The position term of the judge: with a density tolerance no jump can
+    exceed but a correction bound below any correction the network makes,
+    every jump falls back (device-judged and host-judged), the rollout equals
+    the plain method bit for bit, and with the bound far above the largest
+    correction no jump falls back on its account."""
+    import dataclasses
+
+    from warp_sph_gpt_gb300.batch import Case
+    from warp_sph_gpt_gb300.generate import config_small
+    from warp_sph_gpt_gb300.surrogate import LearnedRollout, Network
+
+    base = trained["net"]
+    plain = Case(config_small())
+    plain.run(0, 100)
+    net = Network(dataclasses.replace(base.cfg, tol=1e9, pos_tol=1e-30), "cuda", theta=base.theta.cpu().numpy())
+    case = Case(config_small())
+    ro = LearnedRollout(case, net)
+    ro.native = native
+    stats = ro.run(0, 100)
+    torch.cuda.synchronize()
+    assert stats["jumps"] == 10 and stats["fallbacks"] == 10 and stats["learned_steps"] == 0
+    for a, b in ((plain.P.pos, case.P.pos), (plain.P.vel, case.P.vel), (plain.D.pos, case.D.pos)):
+        np.testing.assert_array_equal(a.cpu().numpy(), b.cpu().numpy())
+    net2 = Network(dataclasses.replace(base.cfg, tol=1e9, pos_tol=1e9), "cuda", theta=base.theta.cpu().numpy())
+    ro2 = LearnedRollout(Case(config_small()), net2)
+    ro2.native = native
+    stats2 = ro2.run(0, 100)
+    assert stats2["fallbacks"] == 0 and 0.0 < stats2["max_pos_accepted"] < 1e-2
+
+
 def test_device_judged_rollout_recovers_from_an_edge_capacity_overflow(trained):
     """A graph that outgrows its edge buffer flags it; the device judge then
     falls back (the plain method runs those steps), and the host grows the

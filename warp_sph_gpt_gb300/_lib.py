@@ -111,7 +111,7 @@ class MpnnGradT(C.Structure):
 class JumpT(C.Structure):
     _fields_ = [("nodes", MpnnNodesT), ("net", MpnnNetT), ("node_grid", GridT), ("scan_scratch", c_int_p),
                 ("graph_ctl", C.c_void_p), ("radius", C.c_float), ("substeps", C.c_int32), ("scale", C.c_float * 4),
-                ("keep", c_float_p), ("dev", c_float_p), ("judge", C.c_int32), ("pad_jump", C.c_int32)]
+                ("keep", c_float_p), ("dev", c_float_p), ("judge", C.c_int32), ("pos_tol", C.c_float)]
 
 
 _MIRRORS = (SphT, BndT, CsrT, DemT, DemBndT, GridT, CtlT, WorkT, ParamsT, CtxT, MpnnNodesT, MpnnNetT, MpnnGradT,

@@ -1539,6 +1539,37 @@ extern "C" int sphdem_mpnn_apply(float* f_pos, float* f_vel, const float* f_acc,
     return launch_status("mpnn_apply");
 }
 
+namespace sd {
+
+// Largest correction displacement of a jump: max over the receivers (fluid
+// rows first, then DEM) of |s_x out[0:3]| + mdt |s_v out[3:6]| into *dst
+// (float bits, atomicMax; values >= 0; *dst starts at 0).
+__global__ void k_corrmax(const float* __restrict__ out, int nf, int nd, float4 sc, float mdt, float* dst) {
+    pdl_wait();
+    pdl_launch();
+    float m = 0.0f;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nf + nd; i += gridDim.x * blockDim.x) {
+        const float sx = i < nf ? sc.x : sc.z, sv = i < nf ? sc.y : sc.w;
+        const float* o = out + 16 * (size_t)i;
+        const float dx = sx * sqrtf(o[0] * o[0] + o[1] * o[1] + o[2] * o[2]);
+        const float dv = sv * sqrtf(o[3] * o[3] + o[4] * o[4] + o[5] * o[5]);
+        m = fmaxf(m, dx + mdt * dv);
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m > 0.0f) atomicMax(reinterpret_cast<int*>(dst), __float_as_int(m));
+}
+
+int run_corrmax(const float* out, int nf, int nd, const float* scale4, float mdt, float* dst, cudaStream_t st) {
+    if (nf + nd <= 0) return SPHDEM_OK;
+    int grid = blocks_for(nf + nd, 256);
+    if (grid > 4 * sm_count()) grid = 4 * sm_count();
+    launch_pdl(k_corrmax, grid, 256, 0, st, out, nf, nd, make_float4(scale4[0], scale4[1], scale4[2], scale4[3]),
+               mdt, dst);
+    return launch_status("jump correction");
+}
+
+}  // namespace sd
+
 extern "C" int sphdem_mpnn_maxdev(const float* a, const float* b, float ref, int32_t n, float inv, float* out,
                                   sphdem_stream_t stream) {
     if (!a || !out || n < 0) {

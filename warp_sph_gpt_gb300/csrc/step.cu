@@ -42,6 +42,7 @@ int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, f
                  int variant = 0);
 int run_interaction_dem(const sphdem_ctx_t* c, float mu, float eps_min, float eps_max, float dt, cudaStream_t st);
 int porosity_setup();
+int run_corrmax(const float* out, int nf, int nd, const float* scale4, float mdt, float* dst, cudaStream_t st);
 int porosity_frame_edge(int frame);
 int64_t porosity_frames(const sphdem_grid_t& g, int F);
 int run_react(const sphdem_ctx_t* c, float support, float dt, bool integrate, cudaStream_t st);
@@ -539,17 +540,21 @@ __global__ void k_keep(KeepArgs a) {
         for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < a.len[s]; i += stride) a.dst[s][i] = a.src[s][i];
 }
 
-// stats: [0] jumps, [1] fallbacks, [2] largest accepted judge value (float
-// bits; values are >= 0), [3] 1 if the last jump fell back.  One thread.
+// stats: [0] jumps, [1] fallbacks, [2] largest accepted density judge value
+// (float bits; values are >= 0), [3] 1 if the last jump fell back, [4]
+// largest accepted position term (float bits).  One thread.
 __global__ void k_decide(const float* __restrict__ dev, const sphdem_ctl_t* __restrict__ gctl, float tol,
-                         cudaGraphConditionalHandle cond, int32_t* __restrict__ stats) {
-    const float d = *dev;
-    const bool fall = !(d <= tol) || gctl->status != 0;  // NaN, or a graph/kernel flag: fall back
+                         float pos_tol, cudaGraphConditionalHandle cond, int32_t* __restrict__ stats) {
+    const float d = dev[0], dx = dev[1];
+    // NaN, a density change above tol, a correction beyond pos_tol, or a graph/kernel flag: fall back
+    const bool fall = !(d <= tol) || (pos_tol > 0.0f && !(dx <= pos_tol)) || gctl->status != 0;
     stats[0] += 1;
-    if (fall)
+    if (fall) {
         stats[1] += 1;
-    else
+    } else {
         stats[2] = max(stats[2], __float_as_int(d));
+        stats[4] = max(stats[4], __float_as_int(dx));
+    }
     stats[3] = fall ? 1 : 0;
     cudaGraphSetConditional(cond, fall ? 1u : 0u);
 }
@@ -712,14 +717,15 @@ int jump_body(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j,
     TRY(sphdem_mpnn_forward(&j->net, 0, st));
     TRY(sphdem_mpnn_apply(c->sph.pos, c->sph.vel, c->sph.acc, c->sph.n, c->dem.pos, c->dem.vel, c->dem.acc,
                           c->dem.n, j->net.out, j->substeps, p->dt, j->scale, nullptr, nullptr, nullptr, st));
-    TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
-    TRY(gather_fluid(c, st));
-    TRY(run_density(c, p->support, p->h, false, true, false, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
-    cudaError_t e = zero_words(j->dev, 1, st);
+    cudaError_t e = zero_words(j->dev, 2, st);
     if (e != cudaSuccess) {
         set_error("jump", e);
         return SPHDEM_ERR_CUDA;
     }
+    TRY(run_corrmax(j->net.out, c->sph.n, c->dem.n, j->scale, (float)j->substeps * p->dt, j->dev + 1, st));
+    TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
+    TRY(gather_fluid(c, st));
+    TRY(run_density(c, p->support, p->h, false, true, false, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
     const float* rho_old = j->keep + 6 * (size_t)c->sph.n + 6 * (size_t)c->dem.n;
     return sphdem_mpnn_maxdev(c->sph.rho, j->judge == 1 ? nullptr : rho_old, p->rho0, c->sph.n, 1.0f / p->rho0,
                               j->dev, st);
@@ -868,7 +874,7 @@ int capture_rollout(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump
     int rc = e == cudaSuccess ? jump_body(c, p, j, shep, fresh, cap) : SPHDEM_ERR_CUDA;
     cudaGraph_t body = nullptr;
     if (!rc) {
-        k_decide<<<1, 1, 0, cap>>>(j->dev, j->graph_ctl, tol, cond, stats);
+        k_decide<<<1, 1, 0, cap>>>(j->dev, j->graph_ctl, tol, j->pos_tol, cond, stats);
         const cudaGraphNode_t* deps = nullptr;
         size_t nd = 0;
         e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, nullptr, &deps, nullptr, &nd);

@@ -54,6 +54,7 @@ class SurrogateConfig:
     norm: float = 32.0             # aggregation normaliser (sum / norm)
     scale: tuple = (1e-4, 1e-1, 1e-4, 1e-1)  # output scales: x fluid, v fluid, x DEM, v DEM
     tol: float = 0.01              # judge tolerance (fraction of rho0)
+    pos_tol: float = 0.0           # > 0: largest correction displacement a jump may apply [m]
     judge: int = 0                 # 0: max change of rho over the jump; 1: max |rho - rho0| / rho0
     edges_per_receiver: int = 160  # initial edge capacity per receiver
 
@@ -114,7 +115,7 @@ class Network:
         c = self.cfg
         return {"theta": self.theta.cpu().numpy(), "radius": c.radius, "dt": c.dt, "rho0": c.rho0,
                 "substeps": c.substeps, "v_scale": c.v_scale, "a_scale": c.a_scale, "norm": c.norm,
-                "scale": np.array(c.scale), "tol": c.tol, "judge": c.judge}
+                "scale": np.array(c.scale), "tol": c.tol, "judge": c.judge, "pos_tol": c.pos_tol}
 
     def save(self, path) -> None:
         np.savez(path, **self.state())
@@ -126,7 +127,8 @@ class Network:
                               substeps=int(z["substeps"]), v_scale=float(z["v_scale"]),
                               a_scale=float(z["a_scale"]), norm=float(z["norm"]),
                               scale=tuple(float(v) for v in z["scale"]), tol=float(z["tol"]),
-                              judge=int(z["judge"]) if "judge" in z else 0)
+                              judge=int(z["judge"]) if "judge" in z else 0,
+                              pos_tol=float(z["pos_tol"]) if "pos_tol" in z else 0.0)
         return Network(cfg, device, theta=z["theta"])
 
 
@@ -631,7 +633,8 @@ def train(net: Network, ts: TrainingSet, members, iters: int, lr: float = 1e-3, 
 def rollout_accounting(stats: dict, counts, m: int, k_jump: int, k_body: int) -> bool:
     """Add one device-judged chunk to ``stats``.  counts = sphdem_rollout's
     device counters [jumps, fallbacks, largest accepted judge value (float
-    bits), last fell back]; every jump ran 1 plain step and every fallback m
+    bits), last fell back, largest accepted position term (float bits)];
+    every jump ran 1 plain step and every fallback m
     more; k_jump / k_body = kernel nodes of the chunk's jump graphs and of
     their fallback bodies (-1: not captured).  Returns whether the number of
     plain steps is odd (each swaps the DEM contact CSR sides once)."""
@@ -642,6 +645,9 @@ def rollout_accounting(stats: dict, counts, m: int, k_jump: int, k_body: int) ->
     stats["plain_steps"] += plain
     stats["learned_steps"] += m * (jumps - fb)
     stats["max_dev_accepted"] = max(stats["max_dev_accepted"], float(np.array(maxbits, np.int32).view(np.float32)))
+    if len(counts) > 4:
+        stats["max_pos_accepted"] = max(stats.get("max_pos_accepted", 0.0),
+                                        float(np.array(int(counts[4]), np.int32).view(np.float32)))
     stats["jump_kernels"] += max(k_jump, 0) + (max(k_body, 0) * fb) // max(jumps, 1)
     return plain % 2 == 1
 
@@ -672,17 +678,17 @@ class LearnedRollout:
         c = case
         self.ctx = context_for(c.P, c.B, c.D, c.W, tuple(c.grids))
         self.keep = torch.zeros(6 * c.P.n + 6 * c.D.n + c.P.n, dtype=torch.float32, device=net.device)
-        self.dev = torch.zeros(1, dtype=torch.float32, device=net.device)
-        self.host = torch.zeros(3, dtype=torch.float32).pin_memory()
+        self.dev = torch.zeros(2, dtype=torch.float32, device=net.device)  # density term, position term
+        self.host = torch.zeros(4, dtype=torch.float32).pin_memory()
         self.jump = None
         self._kernels = {}
         self.last_accepted = False  # the last jump of the last run() was accepted
         self.native = True          # device-judged jumps (sphdem_rollout); False: host-judged
         self._warm = False          # one host-judged jump has run (kernel attributes set)
-        self.dstats = torch.zeros(4, dtype=torch.int32, device=net.device)
-        self.hstats = torch.zeros(4, dtype=torch.int32).pin_memory()
+        self.dstats = torch.zeros(6, dtype=torch.int32, device=net.device)
+        self.hstats = torch.zeros(6, dtype=torch.int32).pin_memory()
         self.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0,
-                          jump_kernels=0)
+                          max_pos_accepted=0.0, jump_kernels=0)
 
     def _setup(self) -> None:
         c, g = self.case, self.g
@@ -704,6 +710,7 @@ class LearnedRollout:
         j.keep = _lib.fptr(self.keep)
         j.dev = _lib.fptr(self.dev)
         j.judge = int(self.cfg.judge)
+        j.pos_tol = float(self.cfg.pos_tol)
         self.jump = j
 
     def run(self, first_step: int, n_steps: int) -> dict:
@@ -791,13 +798,14 @@ class LearnedRollout:
             self.stats["jump_kernels"] += nk
             D._flip("dem")  # the plain step of the jump swapped both contact CSRs
             D._flip("bnd")
-            self.host[0:1].copy_(self.dev, non_blocking=True)
+            self.host[0:1].copy_(self.dev[0:1], non_blocking=True)
             self.host[1:2].copy_(self.g.ctl[3:4], non_blocking=True)
             self.host[2:3].copy_(ctx.ctl[3:4], non_blocking=True)
+            self.host[3:4].copy_(self.dev[1:2], non_blocking=True)
             torch.cuda.current_stream(self.net.device).synchronize()
             self.stats["jumps"] += 1
             self.stats["plain_steps"] += 1
-            dev = float(self.host[0])
+            dev, dpos = float(self.host[0]), float(self.host[3])
             gflags, cflags = int(self.host[1]), int(self.host[2])
             if cflags:
                 ctx._raise_for(cflags)
@@ -808,9 +816,10 @@ class LearnedRollout:
                 self._kernels = {}
             elif gflags:
                 raise RuntimeError(f"learned jump raised device status 0x{gflags:x}")
-            if self.jump is not None and dev <= cfg.tol:
+            if self.jump is not None and dev <= cfg.tol and (cfg.pos_tol <= 0.0 or dpos <= cfg.pos_tol):
                 self.stats["learned_steps"] += m
                 self.stats["max_dev_accepted"] = max(self.stats["max_dev_accepted"], dev)
+                self.stats["max_pos_accepted"] = max(self.stats["max_pos_accepted"], dpos)
                 fresh = 1 if self.reuse_grid else 0
                 self.last_accepted = True
             else:
