@@ -599,7 +599,8 @@ def learned_arm(args, rank, world, local_rank):
     ro.run(0, 6 * K)  # both Shepard variants run eagerly once, then are captured
     torch.cuda.synchronize()
     learned.restore(snapL)
-    ro.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0, jump_kernels=0)
+    ro.stats = dict(jumps=0, fallbacks=0, plain_steps=0, learned_steps=0, max_dev_accepted=0.0, max_pos_accepted=0.0,
+                    jump_kernels=0)
     # e2e: initial state from pinned host memory, final state back to the host
     host_in = {k: t.detach().cpu().pin_memory() for k, t in (("pos", learned.P.pos), ("vel", learned.P.vel),
                                                               ("dpos", learned.D.pos), ("dvel", learned.D.vel))}

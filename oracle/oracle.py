@@ -118,10 +118,12 @@ def set_subject_stride(stride: int) -> None:
 
 
 def _np(t, width):
-    """numpy float32 copy of a torch tensor / array with shape [n, width] or [n]."""
+    """numpy float32 copy of a torch tensor / array with shape [n, width] or [n]
+    (always a copy: two states made from the same CPU tensors must not share
+    memory)."""
     if hasattr(t, "detach"):
         t = t.detach().cpu().numpy()
-    a = np.ascontiguousarray(np.asarray(t, dtype=np.float32))
+    a = np.array(t, dtype=np.float32, order="C", copy=True)
     return a.reshape(-1, width) if width > 1 else a.reshape(-1)
 
 

@@ -99,3 +99,46 @@ def test_neighbour_lists_give_identical_steps(nbr_cap):
             np.testing.assert_array_equal(getattr(part_a, field).cpu().numpy(), getattr(part_b, field).cpu().numpy())
     np.testing.assert_array_equal(ref.P.acc.cpu().numpy(), alt.P.acc.cpu().numpy())
     np.testing.assert_array_equal(ref.P.pgf.cpu().numpy(), alt.P.pgf.cpu().numpy())
+
+
+def test_batch_member_step_matches_oracle():
+    """A member's coupled step inside a batched state against the oracle run on
+    that member alone: fields within max(1e-5, 4 x the FP32 oracle's own error)
+    of FP64, contact CSR bit-exact against the FP32 oracle (as in
+    tests/test_gpu_step_parity.py)."""
+    from oracle.oracle import HostState
+    from test_gpu_step_parity import _compare_csr, _compare_step
+    from warp_sph_gpt_gb300.generate import build_case
+
+    ids = [3, 7, 11]
+    members = _members(ids)
+    ens = Ensemble(members)
+    k = 1  # the middle member: particles before and after it in every set
+    gen, pos, rad = members[k]
+    P, B, D, W = build_case(gen, pos, rad, device="cpu")
+    assert D.n > 0
+    h64, h32 = HostState(P, B, D, W), HostState(P, B, D, W)
+    ens.step(0)
+    torch.cuda.synchronize()
+    h64.sphdem_onestep(ens.solv, 0, ens.scales, p="f64")
+    h32.sphdem_onestep(ens.solv, 0, ens.scales, p="f32")
+
+    class View:  # the member's slice of every field, in the struct's names
+        pass
+
+    views = {}
+    for kind, part in (("sph", ens.P), ("bnd", ens.B), ("dem", ens.D)):
+        v = View()
+        for name, _ in type(part)._fields:
+            setattr(v, name, ens.member(k, kind, name))
+        views[kind] = v
+    _compare_step(ens.solv, views["sph"], views["bnd"], views["dem"], h32, h64)
+    # the member's contact CSR: rows k of the batched CSR, neighbour ids relative to its first sphere
+    o = ens.offsets
+    for kind, wkey in (("dem", "dem"), ("bnd", "dembnd")):
+        off = getattr(ens.D, f"contact_{kind}_offset_old").cpu().numpy()
+        ids_all = getattr(ens.D, f"contact_{kind}_id_old").cpu().numpy()
+        rows = off[o["dem"][k]:o["dem"][k + 1] + 1]
+        ref = h32.side(kind, "old")
+        np.testing.assert_array_equal(rows - rows[0], ref["offset"], err_msg=f"{kind} offsets")
+        np.testing.assert_array_equal(ids_all[rows[0]:rows[-1]] - o[wkey][k], ref["id"], err_msg=f"{kind} ids")

@@ -311,3 +311,17 @@ def test_neighbour_digest_on_lattice():
     assert count.max() == expected == 81
     force, _ = h.neighbour_digest("SPH_SPH_FORCE", s.support)
     np.testing.assert_array_equal(force, count - 1)  # only the particle itself is excluded
+
+
+def test_host_states_do_not_share_memory_with_cpu_tensors():
+    """Two oracle states made from the same CPU structs are independent copies."""
+    import torch
+
+    from oracle.oracle import HostState
+    from warp_sph_gpt_gb300.struct import SPHptl
+
+    P = SPHptl(4, "cpu")
+    P.pos.copy_(torch.arange(12, dtype=torch.float32).reshape(4, 3))
+    a, b = HostState(P), HostState(P)
+    a.sph["pos"][0, 0] = 99.0
+    assert b.sph["pos"][0, 0] == 0.0 and float(P.pos[0, 0]) == 0.0

@@ -351,7 +351,7 @@ __global__ void __launch_bounds__(kPThreads, 2) k_porosity_mma(PorArgs a) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         for (int s = 0; s < kPStages; ++s) {
-            mbar_init(&sh.full[s], kPStageThreads);
+            mbar_init(&sh.full[s], kPStageWarps);
             mbar_init(&sh.empty[s], 1 + kPEpiWarps);
         }
         for (int b = 0; b < 2; ++b) {
@@ -513,9 +513,9 @@ __global__ void __launch_bounds__(kPThreads, 2) k_porosity_mma(PorArgs a) {
             }
             if (warp >= kPMmaWarp + 1) {
                 // ---- staging: candidate rows and volumes ----
-                // thread st builds chunk positions st and st + 64; the
-                // candidates of chunk c + 1 are loaded while chunk c's rows
-                // are built
+                // thread st builds chunk positions st, st + 32 kPStageWarps, ...;
+                // the candidates of chunk c + 1 are loaded while chunk c's
+                // rows are built
                 const int st = tid - 32 * (kPMmaWarp + 1);
                 auto fetch = [&](int c, int t, float4& x) {
                     const int uu = c * kPN + t;
@@ -541,23 +541,25 @@ __global__ void __launch_bounds__(kPThreads, 2) k_porosity_mma(PorArgs a) {
                     store_row(sh.B[s], col, v);
                     sh.V[s][col] = x.w;
                 };
-                float4 x0, x1;
-                if (nchunks > 0) {
-                    fetch(0, st, x0);
-                    fetch(0, st + kPStageThreads, x1);
-                }
+                constexpr int kPerT = kPN / kPStageThreads;  // candidates per staging thread and chunk
+                float4 x[kPerT];
+                if (nchunks > 0)
+#pragma unroll
+                    for (int q = 0; q < kPerT; ++q) fetch(0, st + q * kPStageThreads, x[q]);
                 for (int c = 0; c < nchunks && !sh.abort_flag; ++c) {
                     const uint32_t gi = g + c, s = gi % kPStages, k = gi / kPStages;
                     if (k > 0 && !bwait(&sh.empty[s], (k - 1) & 1u, sh, a.ctl)) break;
-                    float4 y0 = x0, y1 = x1;
-                    if (c + 1 < nchunks) {
-                        fetch(c + 1, st, x0);
-                        fetch(c + 1, st + kPStageThreads, x1);
-                    }
-                    put(s, st, y0);
-                    put(s, st + kPStageThreads, y1);
+                    float4 y[kPerT];
+#pragma unroll
+                    for (int q = 0; q < kPerT; ++q) y[q] = x[q];
+                    if (c + 1 < nchunks)
+#pragma unroll
+                        for (int q = 0; q < kPerT; ++q) fetch(c + 1, st + q * kPStageThreads, x[q]);
+#pragma unroll
+                    for (int q = 0; q < kPerT; ++q) put(s, st + q * kPStageThreads, y[q]);
                     fence_proxy_async_smem();
-                    mbar_arrive(&sh.full[s]);
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&sh.full[s]);  // one arrival per staging warp
                 }
             } else if (warp == kPMmaWarp) {
                 // ---- MMA issue ----

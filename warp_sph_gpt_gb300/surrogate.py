@@ -819,7 +819,7 @@ class LearnedRollout:
             if self.jump is not None and dev <= cfg.tol and (cfg.pos_tol <= 0.0 or dpos <= cfg.pos_tol):
                 self.stats["learned_steps"] += m
                 self.stats["max_dev_accepted"] = max(self.stats["max_dev_accepted"], dev)
-                self.stats["max_pos_accepted"] = max(self.stats["max_pos_accepted"], dpos)
+                self.stats["max_pos_accepted"] = max(self.stats.get("max_pos_accepted", 0.0), dpos)
                 fresh = 1 if self.reuse_grid else 0
                 self.last_accepted = True
             else:
