@@ -340,6 +340,8 @@ def gpu_arm(args, rank, world, local_rank):
             tuning["porosity_variant"] = args.porosity_variant
         if args.nbr_cap >= 0:
             tuning["nbr_cap"] = args.nbr_cap
+        if args.nbr_format >= 0:
+            tuning["nbr_format"] = args.nbr_format
     runner.tune(tuning)
     gen, solv, desc = runner.gen, runner.solv, runner.desc
     P, B, D, W = runner.P, runner.B, runner.D, runner.W
@@ -927,8 +929,10 @@ def main():
     ap.add_argument("--lanes-sph", type=int, default=0, choices=(0, 1, 32),
                     help="threads per particle of the SPH loops (0 = by system size)")
     ap.add_argument("--nbr-cap", type=int, default=-1,
-                    help="neighbour-list capacity between the density and force passes (-1 = sized by the "
-                         "library, 0 = no lists)")
+                    help="neighbour-record capacity between the density and force passes (-1 = sized by the "
+                         "library, 0 = none)")
+    ap.add_argument("--nbr-format", type=int, default=-1, choices=(-1, 0, 1),
+                    help="neighbour records: 0 = member slots, 1 = walk masks (-1 = library default, slots)")
     ap.add_argument("--cell-factor", type=float, default=1.0,
                     help="fluid/wall cell width as a fraction of the SPH support")
     args = ap.parse_args()

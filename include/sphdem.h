@@ -36,7 +36,11 @@
 extern "C" {
 #endif
 
-#define SPHDEM_ABI_VERSION 10
+#define SPHDEM_ABI_VERSION 11
+
+/* work.nbr forms (params.nbr_format): int32 member slots, or walk masks. */
+#define SPHDEM_NBR_SLOTS 0
+#define SPHDEM_NBR_MASKS 1
 
 /* ---- return codes ---------------------------------------------------- */
 #define SPHDEM_OK                0
@@ -201,12 +205,18 @@ typedef struct sphdem_work {
     float* dem_aux;     /* [n_dem,4] 1/h, 21/(16 pi h^3), sqrt bound of 2h, 2h  */
     /* fluid, in grid_sph order, uniform DEM h only */
     float* f_posq;      /* [n_sph,4] x/h, y/h, z/h, m/rho (porosity sums)     */
-    /* fluid neighbour lists written by the density pass and read by the
-     * force pass of the same step, particles in grid_sph order, row-major by
-     * list position so a warp's reads coalesce: rows [0, cap) fluid slots,
-     * rows [cap, 2 cap) wall slots, row 2 cap the fluid count, row 2 cap + 1
-     * the wall count (a count above cap: that particle walks its cells).
-     * cap = params.nbr_cap; NULL or cap 0: no lists. */
+    /* fluid neighbour records written by the density pass and read by the
+     * force pass of the same step, particles in grid_sph order, rows of n_sph
+     * words (particles contiguous within a row, so a warp's accesses
+     * coalesce); rows [0, cap) fluid, rows [cap, 2 cap) wall, rows 2 cap and
+     * 2 cap + 1 the fluid and wall counts.  params.nbr_format chooses the form:
+     *   SPHDEM_NBR_SLOTS: row t holds member t's slot (d2 < support^2, walk
+     *     order); counts = members (above cap: that particle's force pass walks
+     *     its cells);
+     *   SPHDEM_NBR_MASKS: one bit per slot the density pass walks (its
+     *     ball-trimmed cell ranges in walk order), set for a member, 32-bit
+     *     word w in row w; counts = slots walked (above 32 cap: walks).
+     * cap = params.nbr_cap; NULL or cap 0: none, both passes walk. */
     int32_t* nbr;       /* [(2*cap+2), n_sph]                                  */
     /* scratch of the tensor-core porosity pass (porosity_variant 2); sizes from
      * sphdem_porosity_scratch.  NULL: that variant is unavailable. */
@@ -250,7 +260,9 @@ typedef struct sphdem_params {
     int32_t block_sph;
     int32_t porosity_variant;
     int32_t lanes_sph;
-    int32_t nbr_cap;         /* neighbour-list capacity per particle (work.nbr) */
+    int32_t nbr_cap;         /* per particle and kind: slots (SPHDEM_NBR_SLOTS) or
+                                mask words (SPHDEM_NBR_MASKS) of work.nbr       */
+    int32_t nbr_format;      /* SPHDEM_NBR_SLOTS or SPHDEM_NBR_MASKS               */
 } sphdem_params_t;
 
 /* Everything one step touches. */
@@ -409,10 +421,10 @@ int sphdem_neighbour_digest(sphdem_ctx_t* c, int relation, float radius,
  * mix64(neighbour point index)):
  *   DENSITY_FLUID / DENSITY_WALL: the members the density pass recorded in
  *     work.nbr (its d2 < s*s decisions; relations SPH_SPH_SUPPORT and
- *     SPH_BND_SUPPORT); a particle whose list overflowed is digested by the
+ *     SPH_BND_SUPPORT); a particle whose record overflowed is digested by the
  *     same cell walk the force pass then takes;
  *   FORCE_FLUID / FORCE_WALL: the members the force pass sums over (the
- *     recorded lists with 1e-12 < d2, or its own walk when a list overflowed;
+ *     recorded members with 1e-12 < d2, or its own walk when a record overflowed;
  *     relations SPH_SPH_FORCE and SPH_BND_FORCE);
  *   POROSITY_NEAR: count = 1 for the particles the porosity pass listed as
  *     having a DEM within 2 h_b (relation SPH_DEM_2H non-empty), else 0.

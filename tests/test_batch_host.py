@@ -70,20 +70,31 @@ def test_autotune_picks_fastest_and_caches(tmp_path):
 
 
 def test_neighbour_capacity():
-    """The density -> force list capacity: 1.25 x a full support ball + 8,
-    a multiple of 8; an explicit request wins; too large a buffer means none."""
+    """Neighbour-record capacity per particle and kind.  Member slots: 1.25 x
+    a full support ball + 8, a multiple of 8.  Walk masks: 1.25 x the slots of
+    a walk over cells spanning 2 s + c per axis, + 64 bits, in 32-bit words.
+    An explicit request wins; too large a buffer means none."""
     import math
 
+    from warp_sph_gpt_gb300._lib import NBR_MASKS, NBR_SLOTS
     from warp_sph_gpt_gb300.engine import NBR_BYTES_MAX, neighbour_capacity
 
     dx = 0.005
-    cap = neighbour_capacity(792_000, 2.6 * dx, dx ** 3)
+    s = 2.6 * dx
+    cap = neighbour_capacity(792_000, s, dx ** 3)
     ball = 4.0 / 3.0 * math.pi * 2.6 ** 3  # 73.6 particles
+    assert cap == neighbour_capacity(792_000, s, dx ** 3, fmt=NBR_SLOTS)
     assert cap % 8 == 0 and 1.25 * ball + 8 <= cap < 1.25 * ball + 16
-    assert neighbour_capacity(1000, 2.6 * dx, dx ** 3, request=16) == 16
-    assert neighbour_capacity(1000, 2.6 * dx, dx ** 3, request=0) == 0
+    words = neighbour_capacity(792_000, s, dx ** 3, fmt=NBR_MASKS)
+    walked = (3 * 2.6) ** 3  # cell = support: 474.6 slots
+    assert words == math.ceil((1.25 * walked + 64) / 32) == 21
+    half = neighbour_capacity(792_000, s, dx ** 3, cell=0.5 * s, fmt=NBR_MASKS)  # finer cells, shorter walk
+    assert half == math.ceil((1.25 * (2.5 * 2.6) ** 3 + 64) / 32) < words
+    for fmt in (NBR_SLOTS, NBR_MASKS):
+        assert neighbour_capacity(1000, s, dx ** 3, request=16, fmt=fmt) == 16
+        assert neighbour_capacity(1000, s, dx ** 3, request=0, fmt=fmt) == 0
     n_big = NBR_BYTES_MAX // (4 * (2 * cap + 2)) + 1
-    assert neighbour_capacity(n_big, 2.6 * dx, dx ** 3) == 0
+    assert neighbour_capacity(n_big, s, dx ** 3) == 0
 
 
 def test_rollout_accounting():

@@ -4,16 +4,22 @@ Tolerances (stated once, used throughout):
 * neighbour sets and contact CSR (offsets, ids): bit-exact against the FP32
   oracle (reference semantics);
 * whole-step fields: the GPU must be no further from the FP64 oracle than the
-  FP32 oracle itself (the reference's own arithmetic) is, within a factor 4,
-  with a 1e-5 floor:  err(gpu, f64) <= max(1e-5, 4 err(f32, f64)), where err is
+  FP32 oracle itself (the reference's own arithmetic) is, within a factor
+  2.5, with a 1e-5 floor:  err(gpu, f64) <= max(1e-5, 2.5 err(f32, f64)), where err is
   the field-normalised max|a - b| / max|b|.  A whole step chains density ->
   Tait pressure -> force, and near rest B((rho/rho0)^7 - 1) amplifies the
   ~1e-7 FP32 density rounding by the EOS condition number, so a fixed 1e-5 on
   acceleration is not reachable by any FP32 evaluation (the FP32 oracle misses
   it too); pressure is normalised by the bulk modulus K = rho0 c0^2.
   Each kernel on its own meets 1e-5 against FP64 on shared inputs
-  (tests/test_gpu_kernels.py).
+  (tests/test_gpu_kernels.py).  Measured over every comparison of this file,
+  the crops and the batch member, the largest ratio err(gpu)/err(f32) among
+  fields above the floor is 1.95 (DEM force and pressure force), then 1.74
+  (fluid acceleration and velocity): the factor keeps ~25% margin.
 """
+import json
+import os
+
 import numpy as np
 import pytest
 import torch
@@ -27,6 +33,7 @@ from warp_sph_gpt_gb300.kernels import Kernel_step_dem, neighbour_digest
 pytestmark = pytest.mark.gpu
 
 FIELD_TOL = 1e-5
+FIELD_FACTOR = 2.5  # times the FP32 oracle's own error against FP64
 
 
 def _np(t):
@@ -41,9 +48,20 @@ def _err(got, ref, scale_floor=0.0):
     return float(np.abs(got - ref).max() / max(np.abs(ref).max(), scale_floor, 1e-30))
 
 
-def _compare_step(s, P, B, D, h32, h64, tol=FIELD_TOL, factor=4.0):
+def _record(rows):
+    """Per-field errors of a comparison, appended as JSON lines to the file
+    SPHDEM_PARITY_LOG names (unset: not recorded)."""
+    path = os.environ.get("SPHDEM_PARITY_LOG")
+    if path:
+        with open(path, "a") as f:
+            for r in rows:
+                f.write(json.dumps(r) + "\n")
+
+
+def _compare_step(s, P, B, D, h32, h64, tol=FIELD_TOL, factor=FIELD_FACTOR):
     bulk = s.rho0 * s.c0 ** 2
     bad = {}
+    rows = []
     groups = (("sph", P, ("rho", "pres", "acc", "pos", "vel", "porosity", "pgf", "acc_dem", "flt")),
               ("bnd", B, ("rho", "pres")),
               ("dem", D, ("force", "torque", "pos", "vel", "omega", "flt_s", "porosity", "drag", "pressure_force")))
@@ -53,8 +71,11 @@ def _compare_step(s, P, B, D, h32, h64, tol=FIELD_TOL, factor=4.0):
             r64 = getattr(h64, group)[name]
             e_gpu = _err(_np(getattr(obj, name)), r64, floor)
             e_ref = _err(getattr(h32, group)[name], r64, floor)
+            rows.append({"case": os.environ.get("PYTEST_CURRENT_TEST", "").split(" ")[0],
+                         "field": f"{group}.{name}", "gpu": e_gpu, "fp32_oracle": e_ref})
             if not e_gpu <= max(tol, factor * e_ref):
                 bad[f"{group}.{name}"] = (e_gpu, e_ref)
+    _record(rows)
     assert not bad, f"fields beyond max({tol}, {factor} x FP32-oracle error): {bad}"
 
 

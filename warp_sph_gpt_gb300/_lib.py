@@ -71,7 +71,7 @@ class ParamsT(C.Structure):
         ("shepard_step", C.c_int32)] + [(n, C.c_float) for n in (
             "porosity_min", "porosity_max", "radius_max", "boundary_radius_max", "h_max", "h_uniform")] + [
         ("block_sph", C.c_int32), ("porosity_variant", C.c_int32), ("lanes_sph", C.c_int32),
-        ("nbr_cap", C.c_int32)]
+        ("nbr_cap", C.c_int32), ("nbr_format", C.c_int32)]
 
 
 class CtxT(C.Structure):
@@ -122,7 +122,8 @@ FLAG_CSR_DEM_OVERFLOW = 0x1
 FLAG_CSR_BND_OVERFLOW = 0x2
 FLAG_NONFINITE = 0x4
 FLAG_TIMEOUT = 0x10
-ABI_VERSION = 10
+ABI_VERSION = 11
+NBR_SLOTS, NBR_MASKS = 0, 1  # sphdem_params_t.nbr_format
 PHASES = ("grid_sph", "grid_dem", "density", "wall_density", "force", "contacts", "porosity", "exchange",
           "react_integrate", "dem_step")
 POROSITY_SLABS = 8

@@ -21,7 +21,7 @@ from .input_reader import dem_search_scales
 from .simulation import SPHDEM_OneStep, run_steps
 from .struct import BNDptl, DEMBNDptl, DEMptl, SPHptl
 
-TUNING_KEYS = ("block_sph", "porosity_variant", "lanes_sph", "nbr_cap")
+TUNING_KEYS = ("block_sph", "porosity_variant", "lanes_sph", "nbr_cap", "nbr_format")
 _SOLVER_FIELDS = ("h", "support", "rho0", "c0", "gamma", "mu", "g", "dt", "shepard_step", "dem_porosity_min",
                   "dem_porosity_max")
 

@@ -105,57 +105,111 @@ __device__ __forceinline__ void for_each_range(const Geo& g, const Win& w, int i
 // floor(x * inv)), so its horizontal distance to p is at least the square's
 // gap; if it is within rq of p its z lies within sqrt(rq^2 - gap^2) of p.z
 // and its z cell is enumerated.  Face columns extend to infinity (clamping).
-template <class F>
-__device__ __forceinline__ void for_each_range_ball(const Geo& g, float px, float py, float pz, float rq, int inst,
-                                                    F&& f) {
-    const Win w = window(g, px, py, pz, rq);
-    const float rq2 = rq * rq;
-    const float margin = 0.01f * g.cell;
-    const int base_i = inst * g.ncl;
-    for (int cx = w.x0; cx <= w.x1; ++cx) {
-        const float x0 = cx == 0 ? -INFINITY : (float)(g.lo[0] + cx) * g.cell;
-        const float x1 = cx == g.dim[0] - 1 ? INFINITY : (float)(g.lo[0] + cx + 1) * g.cell;
-        const float gx = fmaxf(0.0f, fmaxf(x0 - px, px - x1) - margin);
-        const float gx2 = gx * gx;
-        if (gx2 > rq2) continue;
-        for (int cy = w.y0; cy <= w.y1; ++cy) {
-            const float y0 = cy == 0 ? -INFINITY : (float)(g.lo[1] + cy) * g.cell;
-            const float y1 = cy == g.dim[1] - 1 ? INFINITY : (float)(g.lo[1] + cy + 1) * g.cell;
-            const float gy = fmaxf(0.0f, fmaxf(y0 - py, py - y1) - margin);
-            const float rem = rq2 - gx2 - gy * gy;
-            if (rem < 0.0f) continue;
-            const float zr = sqrtf(rem) + margin;
-            const int z0 = coord(pz - zr, g.inv, g.lo[2], g.dim[2]);
-            const int z1 = coord(pz + zr, g.inv, g.lo[2], g.dim[2]);
-            const int base = base_i + (cx * g.dim[1] + cy) * g.dim[2];
-            const int s = __ldg(g.start + base + z0);
-            const int e = __ldg(g.start + base + z1 + 1);
-            if (s < e) f(s, e);
-        }
-    }
-}
-
-// Slot range [s, e) of column (cx, cy) trimmed to the ball (see above); empty
-// if the column lies beyond rq.
+//
+// column_range_ball gives the slot range [s, e) of column (cx, cy) trimmed to
+// the ball (empty if the column lies beyond rq); for_each_range_ball visits
+// the window's columns x-major.  Every operation is rounded on its own (no
+// contraction), so each kernel that trims a column gets the same range: the
+// density pass's walk masks are decoded against the force pass's own ranges.
 __device__ __forceinline__ void column_range_ball(const Geo& g, int cx, int cy, float px, float py, float pz,
                                                   float rq, int inst, int& s, int& e) {
-    const float margin = 0.01f * g.cell;
-    const float x0 = cx == 0 ? -INFINITY : (float)(g.lo[0] + cx) * g.cell;
-    const float x1 = cx == g.dim[0] - 1 ? INFINITY : (float)(g.lo[0] + cx + 1) * g.cell;
-    const float y0 = cy == 0 ? -INFINITY : (float)(g.lo[1] + cy) * g.cell;
-    const float y1 = cy == g.dim[1] - 1 ? INFINITY : (float)(g.lo[1] + cy + 1) * g.cell;
-    const float gx = fmaxf(0.0f, fmaxf(x0 - px, px - x1) - margin);
-    const float gy = fmaxf(0.0f, fmaxf(y0 - py, py - y1) - margin);
-    const float rem = rq * rq - gx * gx - gy * gy;
+    const float margin = __fmul_rn(0.01f, g.cell);
+    const float x0 = cx == 0 ? -INFINITY : __fmul_rn((float)(g.lo[0] + cx), g.cell);
+    const float x1 = cx == g.dim[0] - 1 ? INFINITY : __fmul_rn((float)(g.lo[0] + cx + 1), g.cell);
+    const float y0 = cy == 0 ? -INFINITY : __fmul_rn((float)(g.lo[1] + cy), g.cell);
+    const float y1 = cy == g.dim[1] - 1 ? INFINITY : __fmul_rn((float)(g.lo[1] + cy + 1), g.cell);
+    const float gx = fmaxf(0.0f, __fsub_rn(fmaxf(__fsub_rn(x0, px), __fsub_rn(px, x1)), margin));
+    const float gy = fmaxf(0.0f, __fsub_rn(fmaxf(__fsub_rn(y0, py), __fsub_rn(py, y1)), margin));
+    const float rem = __fsub_rn(__fsub_rn(__fmul_rn(rq, rq), __fmul_rn(gx, gx)), __fmul_rn(gy, gy));
     s = e = 0;
     if (rem < 0.0f) return;
-    const float zr = sqrtf(rem) + margin;
-    const int z0 = coord(pz - zr, g.inv, g.lo[2], g.dim[2]);
-    const int z1 = coord(pz + zr, g.inv, g.lo[2], g.dim[2]);
+    // MUFU root (its error is far inside the margin); capped at rq, so the
+    // trimmed cells lie within the window's z cells (a member has |dz| < rq)
+    const float zr = fminf(__fadd_rn(__fmul_rn(rem, rsqrtf(fmaxf(rem, 1.0e-30f))), margin), rq);
+    const int z0 = coord(__fsub_rn(pz, zr), g.inv, g.lo[2], g.dim[2]);
+    const int z1 = coord(__fadd_rn(pz, zr), g.inv, g.lo[2], g.dim[2]);
     const int base = inst * g.ncl + (cx * g.dim[1] + cy) * g.dim[2];
     s = __ldg(g.start + base + z0);
     e = __ldg(g.start + base + z1 + 1);
 }
+
+template <class F>
+__device__ __forceinline__ void for_each_range_ball(const Geo& g, float px, float py, float pz, float rq, int inst,
+                                                    F&& f) {
+    const Win w = window(g, px, py, pz, rq);
+    for (int cx = w.x0; cx <= w.x1; ++cx)
+        for (int cy = w.y0; cy <= w.y1; ++cy) {
+            int s, e;
+            column_range_ball(g, cx, cy, px, py, pz, rq, inst, s, e);
+            if (s < e) f(s, e);
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Walk masks.  A pass that walks a subject's ball-trimmed ranges (in the order
+// of for_each_range_ball, each range in slot order) records one bit per slot
+// it walks, set for the members it accepted; word w of a subject's stream sits
+// in row w of a rows x n array (subjects contiguous within a row, so a warp's
+// stores and loads coalesce).  A later pass re-trims the same columns and
+// decodes the bits back into the same member slots in the same order.
+// ---------------------------------------------------------------------------
+// Member slots of a recorded walk, one per next() call, -1 at the end.  Walk
+// positions are consumed in order, so the word holding position b is loaded
+// exactly when b is the first position of a word.
+struct MaskIter {
+    int x1, y0, y1, cx, cy;  // window columns still to trim
+    int cur, end, b;         // unread part of the current range; walk position of cur
+    uint32_t word, m;        // loaded word; unreported members of the current segment
+    int mbase;               // slot of bit 0 of m
+    __device__ __forceinline__ void init(const Geo& g, float px, float py, float pz, float rq) {
+        const Win w = window(g, px, py, pz, rq);
+        x1 = w.x1;
+        y0 = w.y0;
+        y1 = w.y1;
+        cx = w.x0;
+        cy = w.y0 - 1;
+        cur = end = b = 0;
+        word = m = 0u;
+        mbase = 0;
+    }
+    // rows: the stream's cap words per subject (a walk longer than 32 cap ends
+    // early instead of reading past them; the caller only decodes walks that fit)
+    __device__ __forceinline__ int next(const Geo& g, float px, float py, float pz, float rq, int inst,
+                                        const int32_t* __restrict__ rows, size_t n, int k, int cap) {
+        for (;;) {
+            if (m) {
+                const int t = __ffs(m) - 1;
+                m &= m - 1u;
+                return mbase + t;
+            }
+            if (cur < end) {
+                const int sh = b & 31;
+                if (sh == 0) {
+                    if ((b >> 5) >= cap) return -1;
+                    word = (uint32_t)__ldg(rows + (size_t)(b >> 5) * n + k);
+                }
+                const int take = min(32 - sh, end - cur);
+                m = word >> sh;
+                if (take < 32) m &= (1u << take) - 1u;
+                mbase = cur;
+                cur += take;
+                b += take;
+                continue;
+            }
+            for (;;) {
+                if (++cy > y1) {
+                    cy = y0;
+                    if (++cx > x1) {
+                        cx = x1 + 1;
+                        return -1;
+                    }
+                }
+                column_range_ball(g, cx, cy, px, py, pz, rq, inst, cur, end);
+                if (end > cur) break;
+            }
+        }
+    }
+};
 
 // Warp-cooperative ball enumeration: the 32 lanes trim 32 columns at a time
 // (instead of every lane trimming every column), then f(s, e) is called

@@ -17,14 +17,18 @@
 //                    neighbours, same support, one loop.
 //   k_step_sph       Kernel_step_sph (kernel/KERNEL_step.py:6-22).
 //
-// Neighbour lists (one thread per subject): the density pass already decides
-// every fluid-fluid and fluid-wall membership of the step (same support, same
-// exact predicate as the force pass), so it records the member slots in walk
-// order; the force pass then loops over exactly those slots instead of
-// walking its cells again.  A thread walking cells evaluates the force body
-// for ~1 in 5 candidates, and the warp pays for the body on every candidate
-// some lane accepts; from the list every iteration is a member.  Same
-// members, same order, same arithmetic: the forces are bit-identical.
+// Neighbour records (one thread per subject): the density pass already
+// decides every fluid-fluid and fluid-wall membership of the step (same
+// support, same exact predicate as the force pass), so it records them and the
+// force pass loops over exactly those members instead of testing every
+// candidate.  A thread walking cells evaluates the force body for ~1 in 5
+// candidates, and the warp pays for the body on every candidate some lane
+// accepts; from the record every iteration is a member.  Same members, same
+// order, same arithmetic: the forces are bit-identical.  Two forms
+// (params.nbr_format): int32 member slots (SPHDEM_NBR_SLOTS, 4 bytes per
+// member), or walk masks (SPHDEM_NBR_MASKS, one bit per walked slot, ~5 per
+// member: a sixth of the bytes, but the force pass re-trims the ranges and
+// decodes the bits).
 #include "common.cuh"
 
 namespace sd {
@@ -62,6 +66,48 @@ __device__ __forceinline__ float lanes_sum(float v) {
     return LANES == 1 ? v : warp_sum(v);
 }
 
+// Thread-per-subject walk of the ball-trimmed ranges, candidate by candidate
+// (the lanes of a warp, consecutive particles of one or two cells, mostly test
+// the same candidate together, so its load is one broadcast), body(j, q, r)
+// for the members.  With rows, the walk mask is recorded: each range is taken
+// in segments that end where a 32-bit mask word ends, the segment's member
+// bits gathered in a register and stored with the word.  Returns the slots
+// walked.
+template <class Body>
+__device__ __forceinline__ int walk_record(const Geo& g, const float4* __restrict__ posm, const float4& p, float rq,
+                                           int inst, float s2, int32_t* __restrict__ rows, size_t n, int k, int cap,
+                                           Body&& body) {
+    int pos = 0;
+    uint32_t word = 0u;
+    for_each_range_ball(g, p.x, p.y, p.z, rq, inst, [&](int s, int e) {
+        for (int j0 = s; j0 < e;) {
+            const int b = pos + (j0 - s);
+            const int sh = b & 31;
+            const int j1 = min(j0 + 32 - sh, e);
+            uint32_t m = 0u, bit = 1u << sh;
+            for (int j = j0; j < j1; ++j, bit <<= 1) {
+                const float4 q = posm[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 < s2) {
+                    body(j, q, r);
+                    m |= bit;
+                }
+            }
+            if (rows) {
+                word |= m;
+                if (sh + (j1 - j0) == 32) {
+                    if ((b >> 5) < cap) rows[(size_t)(b >> 5) * n + k] = (int32_t)word;
+                    word = 0u;
+                }
+            }
+            j0 = j1;
+        }
+        pos += e - s;
+    });
+    if (rows && (pos & 31) && (pos >> 5) < cap) rows[(size_t)(pos >> 5) * n + k] = (int32_t)word;
+    return pos;
+}
+
 struct DensArgs {
     Geo gs, gb;
     const float4* __restrict__ f_posm;
@@ -73,8 +119,9 @@ struct DensArgs {
     float* pres;
     float4* f_rp;    // out: rho, pres, pres/rho^2, 1/rho  (sorted)
     float4* f_posv;  // out: x, y, z, m/rho                 (sorted)
-    int* nbr;        // out: neighbour lists (sphdem_work_t.nbr), or null
-    int cap;
+    int* nbr;        // out: neighbour records (sphdem_work_t.nbr), or null
+    int cap;         // per subject and kind: slots or mask words
+    int fmt;         // SPHDEM_NBR_SLOTS or SPHDEM_NBR_MASKS
     int n;
     float s2, rq;
     Kern kern;
@@ -92,40 +139,63 @@ __global__ void __launch_bounds__(256) k_density(DensArgs a) {
     const float4 p = a.f_posm[k];
     const int inst = inst_of(a.gs, o);
     float rho_sum = 0.0f, flt_sum = 0.0f;
-    const bool list = LANES == 1 && a.nbr != nullptr;
-    const size_t n = (size_t)a.n;
-    int cf = 0, cb = 0;
-    visit_ball<LANES>(a.gs, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
-        const float4 q = a.f_posm[j];
-        const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-        if (r.d2 < a.s2) {
-            const float w = kern_w(a.kern, fast_sqrt(r.d2));
-            if (RHO) rho_sum += q.w * w;
-            if (FLT) flt_sum += a.f_vprev[j] * w;
-            if (list) {
-                if (cf < a.cap) a.nbr[(size_t)cf * n + k] = j;
-                ++cf;
-            }
-        }
-    });
-    if (a.gb.ncl > 0) {
-        visit_ball<LANES>(a.gb, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
-            const float4 q = a.b_posm[j];
+    if (LANES == 1 && a.nbr != nullptr && a.fmt == SPHDEM_NBR_MASKS) {
+        // the walks, recording their walk masks
+        const size_t n = (size_t)a.n;
+        int32_t* rows = a.nbr;
+        const int wf = walk_record(a.gs, a.f_posm, p, a.rq, inst, a.s2, rows, n, k, a.cap,
+                                   [&](int j, const float4& q, const D2& r) {
+                                       const float w = kern_w(a.kern, fast_sqrt(r.d2));
+                                       if (RHO) rho_sum += q.w * w;
+                                       if (FLT) flt_sum += a.f_vprev[j] * w;
+                                   });
+        int wb = 0;
+        if (a.gb.ncl > 0)
+            wb = walk_record(a.gb, a.b_posm, p, a.rq, inst, a.s2, rows + (size_t)a.cap * n, n, k, a.cap,
+                             [&](int j, const float4& q, const D2& r) {
+                                 const float w = kern_w(a.kern, fast_sqrt(r.d2));
+                                 if (RHO) rho_sum += q.w * w;
+                                 if (FLT) flt_sum += a.b_vprev[j] * w;
+                             });
+        rows[(size_t)(2 * a.cap) * n + k] = wf;
+        rows[(size_t)(2 * a.cap + 1) * n + k] = wb;
+    } else {
+        // the walks, recording the member slots when the step keeps them
+        const bool list = LANES == 1 && a.nbr != nullptr;
+        const size_t n = (size_t)a.n;
+        int cf = 0, cb = 0;
+        visit_ball<LANES>(a.gs, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+            const float4 q = a.f_posm[j];
             const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
             if (r.d2 < a.s2) {
                 const float w = kern_w(a.kern, fast_sqrt(r.d2));
                 if (RHO) rho_sum += q.w * w;
-                if (FLT) flt_sum += a.b_vprev[j] * w;
+                if (FLT) flt_sum += a.f_vprev[j] * w;
                 if (list) {
-                    if (cb < a.cap) a.nbr[(size_t)(a.cap + cb) * n + k] = j;
-                    ++cb;
+                    if (cf < a.cap) a.nbr[(size_t)cf * n + k] = j;
+                    ++cf;
                 }
             }
         });
-    }
-    if (list) {
-        a.nbr[(size_t)(2 * a.cap) * n + k] = cf;
-        a.nbr[(size_t)(2 * a.cap + 1) * n + k] = cb;
+        if (a.gb.ncl > 0) {
+            visit_ball<LANES>(a.gb, p.x, p.y, p.z, a.rq, inst, lane, [&](int j) {
+                const float4 q = a.b_posm[j];
+                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+                if (r.d2 < a.s2) {
+                    const float w = kern_w(a.kern, fast_sqrt(r.d2));
+                    if (RHO) rho_sum += q.w * w;
+                    if (FLT) flt_sum += a.b_vprev[j] * w;
+                    if (list) {
+                        if (cb < a.cap) a.nbr[(size_t)(a.cap + cb) * n + k] = j;
+                        ++cb;
+                    }
+                }
+            });
+        }
+        if (list) {
+            a.nbr[(size_t)(2 * a.cap) * n + k] = cf;
+            a.nbr[(size_t)(2 * a.cap + 1) * n + k] = cb;
+        }
     }
     if (RHO) rho_sum = lanes_sum<LANES>(rho_sum);
     if (FLT) flt_sum = lanes_sum<LANES>(flt_sum);
@@ -200,8 +270,9 @@ struct ForceArgs {
     float* acc;
     float* pgf;
     float4* f_pgf;     // out (sorted): pgf x, y, z, rho
-    const int* nbr;    // neighbour lists of this step's density pass, or null
-    int cap;
+    const int* nbr;    // neighbour records of this step's density pass, or null
+    int cap;           // per subject and kind: slots or mask words
+    int fmt;           // SPHDEM_NBR_SLOTS or SPHDEM_NBR_MASKS
     int n;
     float s2, rq;
     Kern kern;
@@ -236,8 +307,106 @@ __device__ __forceinline__ void force_pair(const ForceArgs& a, const D2& r, cons
     }
 }
 
+// The c member slots rows[t * n + k] recorded for subject k, in walk order,
+// four per round: their slots, then their positions, are loaded together so
+// the gathers overlap (the loop is latency bound).
+template <int MODE>
+__device__ __forceinline__ void force_slots(const ForceArgs& a, const float4* __restrict__ posm,
+                                            const float4* __restrict__ rp, const float4* __restrict__ vel,
+                                            const int32_t* __restrict__ rows, int c, const float4& p,
+                                            const float4& vi, const float4& rpi, int k, float3& acc, float3& pgf) {
+    const size_t n = (size_t)a.n;
+    for (int t = 0; t < c; t += 4) {
+        int js[4];
+        float4 qs[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) js[u] = t + u < c ? rows[(size_t)(t + u) * n + k] : rows[(size_t)t * n + k];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) qs[u] = posm[js[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const D2 r = d2_exact(p.x, p.y, p.z, qs[u].x, qs[u].y, qs[u].z);
+            if (t + u < c && r.d2 > kR2Min)
+                force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, qs[u], rp[js[u]], vel, js[u], acc, pgf);
+        }
+    }
+}
+
+// Ball-trimmed ranges a subject's walk-mask decode keeps in shared memory.
+constexpr int kForceRanges = 16;
+
+// The members a walk mask records for subject k over geometry g, in walk
+// order, summed four per round (their slots, then their positions, are loaded
+// together so the gathers overlap: the loop is latency bound).  The subject's
+// non-empty ball-trimmed ranges are trimmed once into a table in shared memory
+// -- per range, slot - walk position and the walk position where it ends -- so
+// a member costs a find-first-set on its mask word and one table step.
+// Returns false, having summed nothing, when the walk it re-trims is not the
+// one recorded (more ranges than the table holds, or another length): the
+// caller then walks the cells.
+template <int MODE>
+__device__ __forceinline__ bool force_members(const ForceArgs& a, const Geo& g, const float4* __restrict__ posm,
+                                              const float4* __restrict__ rp, const float4* __restrict__ vel,
+                                              const int32_t* __restrict__ rows, int walked, const float4& p,
+                                              const float4& vi, const float4& rpi, int inst, int k, int32_t* tab,
+                                              int ts, float3& acc, float3& pgf) {
+    int nr = 0, pos = 0;
+    for_each_range_ball(g, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
+        if (nr < kForceRanges) {
+            tab[(2 * nr) * ts] = s - pos;  // slot of walk position q in this range: q + (s - pos)
+            tab[(2 * nr + 1) * ts] = pos + (e - s);
+        }
+        ++nr;
+        pos += e - s;
+    });
+    if (nr > kForceRanges || pos != walked) return false;
+    const size_t n = (size_t)a.n;
+    const int nwords = (pos + 31) >> 5;
+    int wi = 0, base = 0, ri = 0;
+    uint32_t word = nwords > 0 ? (uint32_t)__ldg(rows + k) : 0u;
+    int off = nr > 0 ? tab[0] : 0, end = nr > 0 ? tab[ts] : 0;
+    for (bool more = nwords > 0; more;) {
+        int js[4] = {-1, -1, -1, -1};
+#pragma unroll 1
+        for (int u = 0; u < 4;) {
+            if (word == 0u) {
+                if (++wi >= nwords) {
+                    more = false;
+                    break;
+                }
+                word = (uint32_t)__ldg(rows + (size_t)wi * n + k);
+                base = wi << 5;
+                continue;
+            }
+            const int q = base + __ffs(word) - 1;
+            word &= word - 1u;
+            while (q >= end) {
+                ++ri;
+                off = tab[(2 * ri) * ts];
+                end = tab[(2 * ri + 1) * ts];
+            }
+            js[0] = js[1];
+            js[1] = js[2];
+            js[2] = js[3];
+            js[3] = q + off;
+            ++u;
+        }
+        if (js[3] < 0) break;
+        float4 qv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) qv[u] = posm[js[u] < 0 ? js[3] : js[u]];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const D2 r = d2_exact(p.x, p.y, p.z, qv[u].x, qv[u].y, qv[u].z);
+            if (js[u] >= 0 && r.d2 > kR2Min)
+                force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, qv[u], rp[js[u]], vel, js[u], acc, pgf);
+        }
+    }
+    return true;
+}
+
 template <int LANES, int MODE>
-__global__ void __launch_bounds__(256) k_force(ForceArgs a) {
+__global__ void __launch_bounds__(256, 4) k_force(ForceArgs a) {
     pdl_wait();
     pdl_launch();
     int lane;
@@ -250,42 +419,32 @@ __global__ void __launch_bounds__(256) k_force(ForceArgs a) {
     const int inst = inst_of(a.gs, o);
     float3 acc = make_float3(0.f, 0.f, 0.f), pgf = make_float3(0.f, 0.f, 0.f);
     bool walk = true;
-    if (LANES == 1 && a.nbr != nullptr) {
+    if (LANES == 1 && a.nbr != nullptr && a.fmt == SPHDEM_NBR_MASKS) {
         // the members recorded by the density pass (all with d2 < s2), in walk order
+        extern __shared__ int32_t force_tab[];
+        const size_t n = (size_t)a.n;
+        const int wf = a.nbr[(size_t)(2 * a.cap) * n + k], wb = a.nbr[(size_t)(2 * a.cap + 1) * n + k];
+        if (wf <= 32 * a.cap && wb <= 32 * a.cap) {
+            float3 af = acc, pf = pgf;
+            bool ok = force_members<MODE>(a, a.gs, a.f_posm, a.f_rp, a.f_vel, a.nbr, wf, p, vi, rpi, inst, k,
+                                          force_tab + threadIdx.x, blockDim.x, af, pf);
+            if (ok && a.gb.ncl > 0 && wb > 0)
+                ok = force_members<MODE>(a, a.gb, a.b_posm, a.b_rp, a.b_vel, a.nbr + (size_t)a.cap * n, wb, p, vi,
+                                         rpi, inst, k, force_tab + threadIdx.x, blockDim.x, af, pf);
+            if (ok) {
+                walk = false;
+                acc = af;
+                pgf = pf;
+            }
+        }
+    } else if (LANES == 1 && a.nbr != nullptr) {
+        // the member slots recorded by the density pass (all with d2 < s2), in walk order
         const size_t n = (size_t)a.n;
         const int cf = a.nbr[(size_t)(2 * a.cap) * n + k], cb = a.nbr[(size_t)(2 * a.cap + 1) * n + k];
         if (cf <= a.cap && cb <= a.cap) {
             walk = false;
-            // four members per round: their slots, then their positions, are
-            // loaded together so the gathers overlap (the loop is latency bound)
-            for (int t = 0; t < cf; t += 4) {
-                int js[4];
-                float4 qs[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) js[u] = t + u < cf ? a.nbr[(size_t)(t + u) * n + k] : k;
-#pragma unroll
-                for (int u = 0; u < 4; ++u) qs[u] = a.f_posm[js[u]];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const D2 r = d2_exact(p.x, p.y, p.z, qs[u].x, qs[u].y, qs[u].z);
-                    if (t + u < cf && r.d2 > kR2Min)
-                        force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, qs[u], a.f_rp[js[u]], a.f_vel, js[u], acc, pgf);
-                }
-            }
-            for (int t = 0; t < cb; t += 4) {
-                int js[4];
-                float4 qs[4];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) js[u] = t + u < cb ? a.nbr[(size_t)(a.cap + t + u) * n + k] : 0;
-#pragma unroll
-                for (int u = 0; u < 4; ++u) qs[u] = a.b_posm[js[u]];
-#pragma unroll
-                for (int u = 0; u < 4; ++u) {
-                    const D2 r = d2_exact(p.x, p.y, p.z, qs[u].x, qs[u].y, qs[u].z);
-                    if (t + u < cb && r.d2 > kR2Min)
-                        force_pair<MODE>(a, r, vi, rpi.z, rpi.y, rpi.w, qs[u], a.b_rp[js[u]], a.b_vel, js[u], acc, pgf);
-                }
-            }
+            force_slots<MODE>(a, a.f_posm, a.f_rp, a.f_vel, a.nbr, cf, p, vi, rpi, k, acc, pgf);
+            force_slots<MODE>(a, a.b_posm, a.b_rp, a.b_vel, a.nbr + (size_t)a.cap * n, cb, p, vi, rpi, k, acc, pgf);
         }
     }
     if (walk) {
@@ -347,7 +506,7 @@ static float tait_B(float rho0, float c0, float gamma) { return rho0 * c0 * c0 /
 static int launch_block(int b) { return (b == 64 || b == 256) ? b : 128; }
 
 int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
-                float gamma, cudaStream_t st, int block, int lanes, int nbr_cap) {
+                float gamma, cudaStream_t st, int block, int lanes, int nbr_cap, int nbr_format) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     DensArgs a;
@@ -365,6 +524,7 @@ int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rh
     a.f_posv = (float4*)c->work.f_posv;
     a.nbr = (nbr_cap > 0 && lanes != 32) ? c->work.nbr : nullptr;
     a.cap = nbr_cap;
+    a.fmt = nbr_format;
     a.n = n;
     a.s2 = support * support;
     a.rq = pad_radius(support);
@@ -439,7 +599,7 @@ int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, f
 }
 
 int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st, int block,
-              int lanes, int nbr_cap) {
+              int lanes, int nbr_cap, int nbr_format) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     ForceArgs a;
@@ -457,6 +617,7 @@ int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, 
     a.f_pgf = (float4*)c->work.f_pgf;
     a.nbr = (nbr_cap > 0 && lanes != 32) ? c->work.nbr : nullptr;
     a.cap = nbr_cap;
+    a.fmt = nbr_format;
     a.n = n;
     a.s2 = support * support;
     a.rq = pad_radius(support);
@@ -475,12 +636,14 @@ int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, 
             launch_pdl(k_force<32, 1>, nb, bs, 0, st, a);
     } else {
         const int nb = blocks_for(n, bs);
+        const size_t smem =
+            a.nbr && a.fmt == SPHDEM_NBR_MASKS ? (size_t)2 * kForceRanges * bs * sizeof(int32_t) : 0;  // 32 KB at 256
         if (mode == 3)
-            launch_pdl(k_force<1, 3>, nb, bs, 0, st, a);
+            launch_pdl(k_force<1, 3>, nb, bs, smem, st, a);
         else if (mode == 2)
-            launch_pdl(k_force<1, 2>, nb, bs, 0, st, a);
+            launch_pdl(k_force<1, 2>, nb, bs, smem, st, a);
         else
-            launch_pdl(k_force<1, 1>, nb, bs, 0, st, a);
+            launch_pdl(k_force<1, 1>, nb, bs, smem, st, a);
     }
     return launch_status("force");
 }

@@ -27,11 +27,11 @@ int gather_fluid(const sphdem_ctx_t* c, cudaStream_t st);
 int gather_wall(const sphdem_ctx_t* c, float support, float h, cudaStream_t st);
 int gather_wall_rho(const sphdem_ctx_t* c, cudaStream_t st);
 int run_density(const sphdem_ctx_t* c, float support, float h, bool flt, bool rho, bool pres, float rho0, float c0,
-                float gamma, cudaStream_t st, int block = 0, int lanes = 1, int nbr_cap = 0);
+                float gamma, cudaStream_t st, int block = 0, int lanes = 1, int nbr_cap = 0, int nbr_format = 0);
 int run_density_wall(const sphdem_ctx_t* c, float support, float h, bool pres, float rho0, float c0, float gamma,
                      cudaStream_t st, int block = 0, int lanes = 1);
 int run_force(const sphdem_ctx_t* c, float support, float h, float mu, float g, int mode, cudaStream_t st,
-              int block = 0, int lanes = 1, int nbr_cap = 0);
+              int block = 0, int lanes = 1, int nbr_cap = 0, int nbr_format = 0);
 int run_pres(const float* rho, float* pres, int n, float rho0, float c0, float gamma, cudaStream_t st);
 int run_step_sph(const sphdem_ctx_t* c, float dt, cudaStream_t st);
 int run_contacts(const sphdem_ctx_t* c, float radius_max, float bnd_radius_max, float g, float dt, int which,
@@ -78,7 +78,8 @@ namespace {
 // Neighbour lists between the density and force passes of a step, when the
 // context provides their buffer.
 int nbr_cap(const sphdem_ctx_t* c, const sphdem_params_t* p) {
-    return (c->work.nbr != nullptr && p->nbr_cap > 0) ? p->nbr_cap : 0;
+    const bool known = p->nbr_format == SPHDEM_NBR_SLOTS || p->nbr_format == SPHDEM_NBR_MASKS;
+    return (c->work.nbr != nullptr && p->nbr_cap > 0 && known) ? p->nbr_cap : 0;
 }
 
 bool shepard_due(const sphdem_params_t* p, int step) {
@@ -92,11 +93,11 @@ int sph_part(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool write_pg
     if (shep) TRY(gather_wall_rho(c, st));
     const int cap = nbr_cap(c, p);
     TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
-                    cap));
+                    cap, p->nbr_format));
     TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
     sphdem_ctx_t cc = *c;
     if (!write_pgf) cc.sph.pgf = nullptr;
-    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, cap);
+    return run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, cap, p->nbr_format);
 }
 
 int sph_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, bool integrate, cudaStream_t st) {
@@ -189,7 +190,7 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
     TRY(rec(f->wall, f->side3));
     const int cap = nbr_cap(c, p);
     TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
-                    cap));
+                    cap, p->nbr_format));
     TRY(rec(f->dens, st));
     // porosity branch
     TRY(wait(f->side2, f->dens));
@@ -199,7 +200,7 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
     TRY(rec(f->join2, f->side2));
     // main, continued
     TRY(wait(st, f->wall));
-    TRY(run_force(c, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, cap));
+    TRY(run_force(c, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, cap, p->nbr_format));
     TRY(wait(st, f->join));
     TRY(run_interaction_dem(c, p->mu, p->porosity_min, p->porosity_max, p->dt, st));
     TRY(wait(st, f->join2));
@@ -375,8 +376,9 @@ __global__ void k_digest(DigArgs a) {
 }
 
 // Member digests of the hot-path kernels' own decisions (not a re-evaluation
-// of the predicate): the density pass's recorded member lists, the members the
-// force pass takes from them (or, for a particle whose lists overflowed, from
+// of the predicate): the density pass's recorded members (slots or walk
+// masks), the members the force pass takes from them (or, for a particle whose
+// record overflowed, from
 // its own cell walk -- exactly the branch k_force takes), and the porosity
 // pass's near list.  One thread per fluid slot; outputs by point index.
 struct MemArgs {
@@ -384,7 +386,7 @@ struct MemArgs {
     const float4* __restrict__ f_posm;
     const float4* __restrict__ b_posm;
     const int* __restrict__ nbr;
-    int cap, n, which;
+    int cap, fmt, n, which;
     float s2, rq;
     int32_t* count;
     uint64_t* hash;
@@ -398,42 +400,45 @@ __global__ void k_member_digest(MemArgs a) {
     const bool wall = a.which == SPHDEM_MEMBERS_DENSITY_WALL || a.which == SPHDEM_MEMBERS_FORCE_WALL;
     const bool force = a.which == SPHDEM_MEMBERS_FORCE_FLUID || a.which == SPHDEM_MEMBERS_FORCE_WALL;
     const size_t n = (size_t)a.n;
-    int cf = 0, cb = 0;
     bool listed = false;
+    const bool masks = a.fmt == SPHDEM_NBR_MASKS;
     if (a.nbr && a.cap > 0) {
-        cf = a.nbr[(size_t)(2 * a.cap) * n + k];
-        cb = a.nbr[(size_t)(2 * a.cap + 1) * n + k];
-        // the force pass reads both lists only when neither overflowed; the
+        const int cf = a.nbr[(size_t)(2 * a.cap) * n + k];
+        const int cb = a.nbr[(size_t)(2 * a.cap + 1) * n + k];
+        // the force pass reads both records only when neither overflowed; the
         // density pass's record of one kind is complete when it fits
-        listed = force ? (cf <= a.cap && cb <= a.cap) : (wall ? cb <= a.cap : cf <= a.cap);
+        const int lim = masks ? 32 * a.cap : a.cap;
+        listed = force ? (cf <= lim && cb <= lim) : (wall ? cb <= lim : cf <= lim);
     }
     int cnt = 0;
     uint64_t hs = 0;
     const Geo& G = wall ? a.gb : a.gs;
     const float4* q4 = wall ? a.b_posm : a.f_posm;
     auto take = [&](int j) {
+        if (force) {
+            const float4 q = q4[j];
+            const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
+            if (!(r.d2 > kR2Min)) return;
+        }
         ++cnt;
         hs += mix64((uint64_t)G.order[j]);
     };
-    if (listed) {
-        const int c = wall ? cb : cf;
-        const int row0 = wall ? a.cap : 0;
-        for (int t = 0; t < c; ++t) {
-            const int j = a.nbr[(size_t)(row0 + t) * n + k];
-            if (force) {
-                const float4 q = q4[j];
-                const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-                if (!(r.d2 > kR2Min)) continue;
-            }
-            take(j);
-        }
-    } else if (G.ncl > 0) {
-        const int inst = inst_of(a.gs, o);
+    const int inst = inst_of(a.gs, o);
+    const int32_t* rows = a.nbr ? a.nbr + (wall ? (size_t)a.cap * n : 0) : nullptr;
+    if (G.ncl <= 0) {
+    } else if (listed && masks) {
+        MaskIter it;
+        it.init(G, p.x, p.y, p.z, a.rq);
+        for (int j; (j = it.next(G, p.x, p.y, p.z, a.rq, inst, rows, n, k, a.cap)) >= 0;) take(j);
+    } else if (listed) {
+        const int c = a.nbr[(size_t)(2 * a.cap + (wall ? 1 : 0)) * n + k];
+        for (int t = 0; t < c; ++t) take(rows[(size_t)t * n + k]);
+    } else {
         for_each_range_ball(G, p.x, p.y, p.z, a.rq, inst, [&](int s, int e) {
             for (int j = s; j < e; ++j) {
                 const float4 q = q4[j];
                 const D2 r = d2_exact(p.x, p.y, p.z, q.x, q.y, q.z);
-                if (r.d2 < a.s2 && (!force || r.d2 > kR2Min)) take(j);
+                if (r.d2 < a.s2) take(j);
             }
         });
     }
@@ -1010,14 +1015,15 @@ int sphdem_profile_step(sphdem_ctx_t* c, const sphdem_params_t* p, int step, int
         mark();
         if (shep && (rc = gather_wall_rho(c, st))) break;
         if ((rc = run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph,
-                              p->lanes_sph, nbr_cap(c, p))))
+                              p->lanes_sph, nbr_cap(c, p), p->nbr_format)))
             break;
         mark();
         if ((rc = run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph))) break;
         mark();
         sphdem_ctx_t cc = *c;
         if (!coupled) cc.sph.pgf = nullptr;
-        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, nbr_cap(c, p))))
+        if ((rc = run_force(&cc, p->support, p->h, p->mu, p->g, 3, st, p->block_sph, p->lanes_sph, nbr_cap(c, p),
+                            p->nbr_format)))
             break;
         mark();
         if (coupled && (rc = run_contacts(c, p->radius_max, p->boundary_radius_max, p->g, p->dt, 3, st))) break;
@@ -1186,7 +1192,8 @@ int sphdem_member_digest(sphdem_ctx_t* c, const sphdem_params_t* p, int which, i
     a.f_posm = (const float4*)c->work.f_posm;
     a.b_posm = (const float4*)c->work.b_posm;
     a.nbr = c->work.nbr;
-    a.cap = (c->work.nbr != nullptr && p->nbr_cap > 0) ? p->nbr_cap : 0;
+    a.cap = nbr_cap(c, p);
+    a.fmt = p->nbr_format;
     a.n = n;
     a.which = which;
     a.s2 = p->support * p->support;

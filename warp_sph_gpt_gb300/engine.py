@@ -19,17 +19,30 @@ from .grid import HashGrid, empty_grid
 from .struct import BNDptl, DEMBNDptl, DEMptl, SPHptl
 
 KIND_SPH, KIND_BND, KIND_DEM, KIND_DEMBND = 0, 1, 2, 3
-NBR_BYTES_MAX = 16 << 30  # neighbour lists above this size are not kept (the passes walk cells)
+NBR_BYTES_MAX = 16 << 30  # neighbour records above this size are not kept (the force pass walks cells)
 
 
-def neighbour_capacity(n: int, support: float, mean_volume: float, request: int = -1) -> int:
-    """Per-particle capacity of the density -> force neighbour lists: by
-    default 1.25 x the particles a full support ball holds at the mean
-    particle volume, + 8, rounded up to a multiple of 8; ``request`` >= 0 sets
-    it (0 = no lists).  0 when (2 cap + 2) n words exceed NBR_BYTES_MAX."""
+def neighbour_capacity(n: int, support: float, mean_volume: float, request: int = -1, cell: float = 0.0,
+                       fmt: int = _lib.NBR_SLOTS) -> int:
+    """Per-particle capacity of each kind's density -> force neighbour record
+    (``request`` >= 0 sets it; 0 = none).  Member slots (NBR_SLOTS): 1.25 x
+    the particles a full support ball holds at the mean particle volume, + 8,
+    rounded up to a multiple of 8.  Walk masks (NBR_MASKS): 32-bit words for
+    1.25 x the slots one walk visits -- the cells overlapping [p - s, p + s]
+    span 2 s + c per axis on average (s = support, c = cell width, the support
+    when 0) -- + 64 bits.  0 when the (2 cap + 2) n words exceed
+    NBR_BYTES_MAX.  A
+    particle whose record overflows has its force pass walk its cells (same
+    results)."""
     cap = max(0, int(request))
     if request < 0 and mean_volume > 0.0:
-        cap = 8 * math.ceil((1.25 * 4.0 / 3.0 * math.pi * support ** 3 / mean_volume + 8.0) / 8.0)
+        ball = 4.0 / 3.0 * math.pi * support ** 3 / mean_volume
+        if fmt == _lib.NBR_MASKS:
+            c = cell if cell > 0.0 else support
+            walked = (2.0 * support + c) ** 3 / mean_volume
+            cap = math.ceil((1.25 * walked + 64.0) / 32.0)
+        else:
+            cap = 8 * math.ceil((1.25 * ball + 8.0) / 8.0)
     return 0 if (2 * cap + 2) * n * 4 > NBR_BYTES_MAX else cap
 
 
@@ -78,7 +91,8 @@ class StepContext:
         self._status_host = torch.zeros(16, dtype=torch.int32, pin_memory=True)
         self._status_event = None
         # launch tuning (results do not depend on it): see autotune.py
-        self.tuning = {"block_sph": 0, "porosity_variant": 2, "lanes_sph": 1, "nbr_cap": -1}
+        self.tuning = {"block_sph": 0, "porosity_variant": 2, "lanes_sph": 1, "nbr_cap": -1,
+                       "nbr_format": _lib.NBR_SLOTS}
         self._nbr_key = None
         self._nbr_cap = 0
         self._mean_vol = 0.0
@@ -100,17 +114,22 @@ class StepContext:
             dem_count=torch.zeros(2 * (nd + 1), **i), dem_aux=torch.zeros((nd, 4), **f),
             f_posq=torch.zeros((ns, 4), **f), nbr=torch.zeros(1, **i))
 
-    def _neighbour_lists(self, solv, request: int = -1) -> int:
-        """Neighbour-list capacity (neighbour_capacity, mean particle volume
-        m / rho0) and buffer, allocated once per (support, rho0, request).
-        Particles with more members walk their cells (same results)."""
-        P = self.sets[0]
-        key = (float(solv.support), float(solv.rho0), int(request))
+    def _neighbour_lists(self, solv, request: int = -1, fmt: int = _lib.NBR_SLOTS) -> int:
+        """Neighbour-record capacity (neighbour_capacity at the smaller of the
+        fluid and wall mean particle volumes m / rho0 and the fluid-grid cell
+        width) and buffer, allocated once per (support, rho0, cell, request,
+        format)."""
+        P, B = self.sets[0], self.sets[1]
+        g = self.grids[0]
+        cell = float(g.radius) * float(g.cell_factor) if g.radius else 0.0
+        key = (float(solv.support), float(solv.rho0), cell, int(request), int(fmt))
         if P.n == 0 or key == self._nbr_key:
             return self._nbr_cap
-        vol = float(P.m.double().mean().item()) / key[1]  # one host sync per key
+        vol = float(P.m.double().mean().item()) / key[1]  # host syncs once per key
         self._mean_vol = vol
-        cap = neighbour_capacity(P.n, key[0], vol if request < 0 else 0.0, request)
+        if B is not None and B.n > 0:
+            vol = min(vol, float(B.m.double().mean().item()) / key[1])
+        cap = neighbour_capacity(P.n, key[0], vol if request < 0 else 0.0, request, cell, fmt)
         self.work["nbr"] = (torch.zeros((2 * cap + 2) * P.n, dtype=torch.int32, device=self.device) if cap
                             else torch.zeros(1, dtype=torch.int32, device=self.device))
         self._nbr_key, self._nbr_cap = key, cap
@@ -246,7 +265,9 @@ class StepContext:
         p.block_sph = int(self.tuning.get("block_sph", 0))
         p.porosity_variant = int(self.tuning.get("porosity_variant", 0))
         p.lanes_sph = int(self.tuning.get("lanes_sph", 1))
-        p.nbr_cap = self._neighbour_lists(solv, int(self.tuning.get("nbr_cap", -1)))
+        fmt = int(self.tuning.get("nbr_format", _lib.NBR_SLOTS))
+        p.nbr_cap = self._neighbour_lists(solv, int(self.tuning.get("nbr_cap", -1)), fmt)
+        p.nbr_format = fmt
 
     @property
     def stream(self):
