@@ -599,14 +599,18 @@ CplArgs make_args(const sphdem_ctx_t* c, float support, float h) {
 
 }  // namespace
 
-int run_porosity_mma(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st);
+int run_porosity_mma(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st,
+                     int part);
 
+// part 0: the whole pass; 1: what depends on positions only (the tensor-core
+// pass's near flags and tiles; nothing for the other variants); 2: the rest.
 int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st,
-                 int variant) {
+                 int variant, int part) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     // the tensor-core normaliser serves a uniform DEM h (variant 2)
-    if (variant == 2 && h > 0.0f && c->dem.n > 0) return run_porosity_mma(c, support, h, eps_min, eps_max, st);
+    if (variant == 2 && h > 0.0f && c->dem.n > 0) return run_porosity_mma(c, support, h, eps_min, eps_max, st, part);
+    if (part == 1) return SPHDEM_OK;
     CplArgs a = make_args(c, support, h);
     a.eps_min = eps_min;
     a.eps_max = eps_max;

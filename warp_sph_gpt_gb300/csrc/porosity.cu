@@ -107,6 +107,7 @@ constexpr uint32_t kPSmemBytes = (sizeof(PorSmem) + 1024 > 80u * 1024u) ? (uint3
 
 struct PorArgs {
     Geo gs, gd;
+    const float4* __restrict__ f_posm;  // x, y, z, m (fluid, grid order; the near flags read these)
     const float4* __restrict__ f_posv;  // x, y, z, m/rho (fluid, grid order)
     const float4* __restrict__ aux;     // per DEM: 1/h, cw, sqrt bound of 2h, 2h
     sphdem_sph_t P;
@@ -214,7 +215,7 @@ __global__ void __launch_bounds__(256) k_pnear(PorArgs a) {
     const int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= a.P.n) return;
     const int o = a.gs.order[k];
-    const float4 p = a.f_posv[k];
+    const float4 p = a.f_posm[k];  // positions only: runs before the density pass is done
     const int key = a.gs.key[o];
     const int inst = a.gs.ncl > 0 ? key / a.gs.ncl : 0;
     bool near = false;
@@ -713,7 +714,11 @@ int porosity_setup() { return smem_opt_in_porosity(); }
 // The tensor-core porosity pass (uniform DEM h > 0) with the frame-block
 // edge its scratch was sized for.  Returns SPHDEM_ERR_INVALID when the
 // context lacks those buffers.
-int run_porosity_mma(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st) {
+// part 0: the whole pass; 1: the near flags and tiles (k_pnear, k_plist: they
+// read positions only, so they may run while the density pass runs); 2: the
+// normaliser and the finish (after the density pass and part 1).
+int run_porosity_mma(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st,
+                     int part) {
     const int n = c->sph.n;
     if (n <= 0) return SPHDEM_OK;
     const sphdem_work_t& w = c->work;
@@ -729,6 +734,7 @@ int run_porosity_mma(const sphdem_ctx_t* c, float support, float h, float eps_mi
     PorArgs a;
     a.gs = make_geo(c->grid_sph);
     a.gd = make_geo(c->grid_dem);
+    a.f_posm = (const float4*)w.f_posm;
     a.f_posv = (const float4*)w.f_posv;
     a.aux = (const float4*)w.dem_aux;
     a.P = c->sph;
@@ -755,21 +761,25 @@ int run_porosity_mma(const sphdem_ctx_t* c, float support, float h, float eps_mi
     const int span = (int)ceilf(2.0f * a.rq / cell) + F + 3;
     a.Wx = (span + kPSlabs - 2) / (kPSlabs - 1);
     if (a.Wx < 1) a.Wx = 1;
-    // counters: listed particles, work units, tiles, listed frame blocks,
-    // evaluated chunks (control words 6..10)
-    cudaError_t e = zero_words(&c->ctl->n_near, 5, st);
-    if (e == cudaSuccess) e = zero_words(a.cnt, nfb, st);
-    if (e != cudaSuccess) {
-        set_error("porosity memset", e);
-        return SPHDEM_ERR_CUDA;
-    }
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    launch_pdl(k_pnear, blocks_for(n, 256), 256, 0, st, a);
-    launch_pdl(k_plist, 8 * sms, 256, 0, st, a);
-    launch_pdl(k_porosity_mma, 2 * sms, kPThreads, kPSmemBytes, st, a);
-    launch_pdl(k_pfinish, blocks_for(n, 256), 256, 0, st, a);
+    if (part != 2) {
+        // counters: listed particles, work units, tiles, listed frame blocks,
+        // evaluated chunks (control words 6..10)
+        cudaError_t e = zero_words(&c->ctl->n_near, 5, st);
+        if (e == cudaSuccess) e = zero_words(a.cnt, nfb, st);
+        if (e != cudaSuccess) {
+            set_error("porosity memset", e);
+            return SPHDEM_ERR_CUDA;
+        }
+        launch_pdl(k_pnear, blocks_for(n, 256), 256, 0, st, a);
+        launch_pdl(k_plist, 8 * sms, 256, 0, st, a);
+    }
+    if (part != 1) {
+        launch_pdl(k_porosity_mma, 2 * sms, kPThreads, kPSmemBytes, st, a);
+        launch_pdl(k_pfinish, blocks_for(n, 256), 256, 0, st, a);
+    }
     return launch_status("porosity (tensor cores)");
 }
 

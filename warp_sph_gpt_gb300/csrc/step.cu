@@ -39,7 +39,7 @@ int run_contacts(const sphdem_ctx_t* c, float radius_max, float bnd_radius_max, 
 int run_dem_aux(const sphdem_ctx_t* c, cudaStream_t st);
 int run_step_dem(const sphdem_ctx_t* c, float dt, cudaStream_t st);
 int run_porosity(const sphdem_ctx_t* c, float support, float h, float eps_min, float eps_max, cudaStream_t st,
-                 int variant = 0);
+                 int variant = 0, int part = 0);
 int run_interaction_dem(const sphdem_ctx_t* c, float mu, float eps_min, float eps_max, float dt, cudaStream_t st);
 int porosity_setup();
 int run_corrmax(const float* out, int nf, int nd, const float* scale4, float mdt, float* dst, cudaStream_t st);
@@ -192,11 +192,14 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
     TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
                     cap, p->nbr_format));
     TRY(rec(f->dens, st));
-    // porosity branch
-    TRY(wait(f->side2, f->dens));
-    TRY(wait(f->side2, f->ready));
+    // porosity branch: what needs positions only (the sorted copies and the
+    // DEM grid) runs beside the density pass, the normaliser after it
     const float support = 2.0f * p->h_max;  // source/Simulation.py:208
-    TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, f->side2, p->porosity_variant));
+    TRY(wait(f->side2, f->fork2));
+    TRY(wait(f->side2, f->ready));
+    TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, f->side2, p->porosity_variant, 1));
+    TRY(wait(f->side2, f->dens));
+    TRY(run_porosity(c, support, p->h_uniform, p->porosity_min, p->porosity_max, f->side2, p->porosity_variant, 2));
     TRY(rec(f->join2, f->side2));
     // main, continued
     TRY(wait(st, f->wall));
