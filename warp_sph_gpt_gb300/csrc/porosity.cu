@@ -300,49 +300,107 @@ __device__ __forceinline__ bool bwait(uint64_t* bar, uint32_t parity, PorSmem& s
     return false;
 }
 
-// 32 columns of this thread's TMEM lane, loaded and waited for in one
-// statement (the registers are defined only once the data has landed).
-__device__ __forceinline__ void ld32(uint32_t taddr, uint32_t* r) {
+// 16 columns of this thread's TMEM lane, loaded and waited for in one statement.
+__device__ __forceinline__ void ld16(uint32_t taddr, uint32_t* r) {
     asm volatile(
-        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
-        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
-        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n\t"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n\t"
         "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
-          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
-          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
         : "r"(taddr)
         : "memory");
 }
 
-// The weighted sums of 32 chunk columns starting at a multiple of 32: column
-// 4i + c holds a candidate of class c (or c + 4 in the second half of the
-// chunk) and goes to accumulator c.  u^4 (1 + 2q), u = 1 - q/2, is evaluated
-// as the expanded polynomial 1 + s (-5/2 + q (5/2 + q (-15/16 + q/8))) with s
-// = q^2 clamped to [0, 4]: every Horner step is exact at q = 2, so the weight
-// there is exactly 0.  The polynomial and the sums run on packed FP32 pairs
-// (fma.rn.f32x2: two independent round-to-nearest FMAs, the values of the
-// scalar ones).
-__device__ __forceinline__ void sums32(const uint32_t* r, const float* V, float2& a01, float2& a23) {
-    const float2 k0 = make_float2(0.125f, 0.125f), k1 = make_float2(-0.9375f, -0.9375f);
-    const float2 k2 = make_float2(2.5f, 2.5f), k3 = make_float2(-2.5f, -2.5f), one = make_float2(1.0f, 1.0f);
-    const float4* V4 = reinterpret_cast<const float4*>(V);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        const float s0 = fminf(fabsf(__uint_as_float(r[4 * i])), 4.0f);
-        const float s1 = fminf(fabsf(__uint_as_float(r[4 * i + 1])), 4.0f);
-        const float s2 = fminf(fabsf(__uint_as_float(r[4 * i + 2])), 4.0f);
-        const float s3 = fminf(fabsf(__uint_as_float(r[4 * i + 3])), 4.0f);
-        const float4 v = V4[i];
-        const float2 sa = make_float2(s0, s1), sb = make_float2(s2, s3);
-        const float2 qa = make_float2(sqrt_apx(s0), sqrt_apx(s1)), qb = make_float2(sqrt_apx(s2), sqrt_apx(s3));
-        const float2 ca = __ffma2_rn(__ffma2_rn(__ffma2_rn(k0, qa, k1), qa, k2), qa, k3);
-        const float2 cb = __ffma2_rn(__ffma2_rn(__ffma2_rn(k0, qb, k1), qb, k2), qb, k3);
-        a01 = __ffma2_rn(make_float2(v.x, v.y), __ffma2_rn(ca, sa, one), a01);
-        a23 = __ffma2_rn(make_float2(v.z, v.w), __ffma2_rn(cb, sb, one), a23);
-    }
+// The polynomial's packed constants as 64-bit register pairs.
+struct Kpk {
+    unsigned long long k0, k1, k2, k3, one;
+};
+__device__ __forceinline__ unsigned long long pk2(float a) {
+    return ((unsigned long long)__float_as_uint(a) << 32) | __float_as_uint(a);
 }
+
+// The weighted sums of 16 chunk columns r (s_ij bits of this thread's
+// subject): column 4i + c holds a candidate of class c (or c + 4 in the second
+// half of the chunk) and goes to accumulator c (a01 holds classes 0-1, a23
+// classes 2-3, as FP32 pairs).  u^4 (1 + 2q), u = 1 - q/2, is evaluated as the
+// expanded polynomial 1 + s (-5/2 + q (5/2 + q (-15/16 + q/8))) with s = q^2
+// clamped to [0, 4] (|s| first: the MMA's rounding can leave a coincident pair
+// slightly negative): every Horner step is exact at q = 2, so the weight there
+// is exactly 0.  The polynomial and the sums run on packed FP32 pairs
+// (fma.rn.ftz.f32x2: two independent round-to-nearest FMAs); V (candidate
+// volumes, 0 for padding) is read from shared memory at vaddr.
+//
+// sums16_next is one statement that first issues the load of the lane's next
+// 16 columns into s and ends with the wait for it: the arithmetic reads only
+// registers that are not the load's destination, and nothing outside the
+// statement sees s before the data has landed, so the load's latency hides
+// behind the arithmetic without a register of a load in flight ever being
+// read, moved or spilled.
+// PTX of four columns: operands R0..R3 hold their s bits, V the shared-memory
+// address of the chunk's volumes, OFF the byte offset of these four, A01/A23
+// the accumulators, K0..K3/ONE the packed polynomial constants.
+#define POR_SUMS4(R0, R1, R2, R3, V, OFF, A01, A23, K0, K1, K2, K3, ONE)                              \
+    "mov.b32 s0, %" #R0 ";\n\tmov.b32 s1, %" #R1 ";\n\tmov.b32 s2, %" #R2 ";\n\tmov.b32 s3, %" #R3 ";\n\t" \
+    "abs.ftz.f32 s0, s0;\n\tabs.ftz.f32 s1, s1;\n\tabs.ftz.f32 s2, s2;\n\tabs.ftz.f32 s3, s3;\n\t"        \
+    "min.ftz.f32 s0, s0, 0f40800000;\n\tmin.ftz.f32 s1, s1, 0f40800000;\n\t"                           \
+    "min.ftz.f32 s2, s2, 0f40800000;\n\tmin.ftz.f32 s3, s3, 0f40800000;\n\t"                           \
+    "sqrt.approx.ftz.f32 q0, s0;\n\tsqrt.approx.ftz.f32 q1, s1;\n\t"                                    \
+    "sqrt.approx.ftz.f32 q2, s2;\n\tsqrt.approx.ftz.f32 q3, s3;\n\t"                                    \
+    "mov.b64 sa, {s0, s1};\n\tmov.b64 sb, {s2, s3};\n\tmov.b64 qa, {q0, q1};\n\tmov.b64 qb, {q2, q3};\n\t" \
+    "fma.rn.ftz.f32x2 ca, %" #K0 ", qa, %" #K1 ";\n\tfma.rn.ftz.f32x2 cb, %" #K0 ", qb, %" #K1 ";\n\t"   \
+    "fma.rn.ftz.f32x2 ca, ca, qa, %" #K2 ";\n\tfma.rn.ftz.f32x2 cb, cb, qb, %" #K2 ";\n\t"               \
+    "fma.rn.ftz.f32x2 ca, ca, qa, %" #K3 ";\n\tfma.rn.ftz.f32x2 cb, cb, qb, %" #K3 ";\n\t"               \
+    "fma.rn.ftz.f32x2 wa, ca, sa, %" #ONE ";\n\tfma.rn.ftz.f32x2 wb, cb, sb, %" #ONE ";\n\t"             \
+    "ld.shared.v4.f32 {v0, v1, v2, v3}, [%" #V "+" #OFF "];\n\t"                                         \
+    "mov.b64 va, {v0, v1};\n\tmov.b64 vb, {v2, v3};\n\t"                                                \
+    "fma.rn.ftz.f32x2 %" #A01 ", va, wa, %" #A01 ";\n\tfma.rn.ftz.f32x2 %" #A23 ", vb, wb, %" #A23 ";\n\t"
+#define POR_REGS                          \
+    ".reg .f32 s<4>, q<4>, v<4>;\n\t"     \
+    ".reg .b64 sa, sb, qa, qb, ca, cb, va, vb, wa, wb;\n\t"
+
+// Operands: %0-%15 s (next columns), %16/%17 a01/a23, %18-%33 r, %34 vaddr,
+// %35 the next columns' TMEM address, %36-%40 the constants.
+__device__ __forceinline__ void sums16_next(const uint32_t* r, uint32_t vaddr, uint32_t tnext, uint32_t* s,
+                                            unsigned long long& a01, unsigned long long& a23, const Kpk& K) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%35];\n\t"
+        "{\n\t" POR_REGS
+        POR_SUMS4(18, 19, 20, 21, 34, 0, 16, 17, 36, 37, 38, 39, 40)
+        POR_SUMS4(22, 23, 24, 25, 34, 16, 16, 17, 36, 37, 38, 39, 40)
+        POR_SUMS4(26, 27, 28, 29, 34, 32, 16, 17, 36, 37, 38, 39, 40)
+        POR_SUMS4(30, 31, 32, 33, 34, 48, 16, 17, 36, 37, 38, 39, 40)
+        "}\n\t"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(s[0]), "=r"(s[1]), "=r"(s[2]), "=r"(s[3]), "=r"(s[4]), "=r"(s[5]), "=r"(s[6]), "=r"(s[7]),
+          "=r"(s[8]), "=r"(s[9]), "=r"(s[10]), "=r"(s[11]), "=r"(s[12]), "=r"(s[13]), "=r"(s[14]), "=r"(s[15]),
+          "+l"(a01), "+l"(a23)
+        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+          "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(vaddr),
+          "r"(tnext), "l"(K.k0), "l"(K.k1), "l"(K.k2), "l"(K.k3), "l"(K.one)
+        : "memory");
+}
+
+// The same arithmetic on the last 16 columns of a chunk half (no load behind
+// it).  Operands: %0/%1 a01/a23, %2-%17 r, %18 vaddr, %19-%23 the constants.
+__device__ __forceinline__ void sums16(const uint32_t* r, uint32_t vaddr, unsigned long long& a01,
+                                       unsigned long long& a23, const Kpk& K) {
+    asm volatile(
+        "{\n\t" POR_REGS
+        POR_SUMS4(2, 3, 4, 5, 18, 0, 0, 1, 19, 20, 21, 22, 23)
+        POR_SUMS4(6, 7, 8, 9, 18, 16, 0, 1, 19, 20, 21, 22, 23)
+        POR_SUMS4(10, 11, 12, 13, 18, 32, 0, 1, 19, 20, 21, 22, 23)
+        POR_SUMS4(14, 15, 16, 17, 18, 48, 0, 1, 19, 20, 21, 22, 23)
+        "}"
+        : "+l"(a01), "+l"(a23)
+        : "r"(r[0]), "r"(r[1]), "r"(r[2]), "r"(r[3]), "r"(r[4]), "r"(r[5]), "r"(r[6]), "r"(r[7]), "r"(r[8]),
+          "r"(r[9]), "r"(r[10]), "r"(r[11]), "r"(r[12]), "r"(r[13]), "r"(r[14]), "r"(r[15]), "r"(vaddr),
+          "l"(K.k0), "l"(K.k1), "l"(K.k2), "l"(K.k3), "l"(K.one)
+        : "memory");
+}
+#undef POR_SUMS4
+#undef POR_REGS
 
 __global__ void __launch_bounds__(kPThreads, 2) k_porosity_mma(PorArgs a) {
     pdl_wait();
@@ -594,11 +652,21 @@ __global__ void __launch_bounds__(kPThreads, 2) k_porosity_mma(PorArgs a) {
                     // other epilogue warps of the sub-partition hide each load
                     const int h0 = (warp >> 2) * (kPN / 2);
                     const uint32_t tcol = tmem + ((uint32_t)(32 * (warp & 3)) << 16) + b * kPN + h0;
-#pragma unroll 1
-                    for (int kc = 0; kc < kPN / 2; kc += 32) {
-                        uint32_t r[32];
-                        ld32(tcol + kc, r);
-                        sums32(r, &sh.V[s][h0 + kc], acc01, acc23);
+                    {
+                        // 16 columns per step, the load of the next 16 behind the arithmetic
+                        const Kpk K{pk2(0.125f), pk2(-0.9375f), pk2(2.5f), pk2(-2.5f), pk2(1.0f)};
+                        const uint32_t va = (uint32_t)__cvta_generic_to_shared(&sh.V[s][h0]);
+                        unsigned long long u01, u23;
+                        memcpy(&u01, &acc01, 8);
+                        memcpy(&u23, &acc23, 8);
+                        uint32_t r0[16], r1[16];
+                        ld16(tcol, r0);
+                        sums16_next(r0, va, tcol + 16, r1, u01, u23, K);
+                        sums16_next(r1, va + 64, tcol + 32, r0, u01, u23, K);
+                        sums16_next(r0, va + 128, tcol + 48, r1, u01, u23, K);
+                        sums16(r1, va + 192, u01, u23, K);
+                        memcpy(&acc01, &u01, 8);
+                        memcpy(&acc23, &u23, 8);
                     }
                     umma::fence_before();
                     __syncwarp();
