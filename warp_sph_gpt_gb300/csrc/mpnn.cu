@@ -68,6 +68,13 @@ __device__ __forceinline__ uint32_t pack2(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
     return *reinterpret_cast<uint32_t*>(&h);
 }
+// max(a, 0), max(b, 0) rounded to BF16 and packed (a in the low half), one
+// instruction.
+__device__ __forceinline__ uint32_t pack2_relu(float a, float b) {
+    uint32_t r;
+    asm("cvt.rn.relu.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(b), "f"(a));
+    return r;
+}
 __device__ __forceinline__ uint16_t bf16_bits(float a) {
     __nv_bfloat16 h = __float2bfloat16_rn(a);
     return *reinterpret_cast<uint16_t*>(&h);
@@ -502,10 +509,10 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
             for (int q = 0; q < 4; ++q) {
                 const int k = c0 + 8 * q;
                 uint4 w;
-                w.x = pack2(fmaxf(v[8 * q], 0.f), fmaxf(v[8 * q + 1], 0.f));
-                w.y = pack2(fmaxf(v[8 * q + 2], 0.f), fmaxf(v[8 * q + 3], 0.f));
-                w.z = pack2(fmaxf(v[8 * q + 4], 0.f), fmaxf(v[8 * q + 5], 0.f));
-                w.w = pack2(fmaxf(v[8 * q + 6], 0.f), fmaxf(v[8 * q + 7], 0.f));
+                w.x = pack2_relu(v[8 * q], v[8 * q + 1]);
+                w.y = pack2_relu(v[8 * q + 2], v[8 * q + 3]);
+                w.z = pack2_relu(v[8 * q + 4], v[8 * q + 5]);
+                w.w = pack2_relu(v[8 * q + 6], v[8 * q + 7]);
                 *reinterpret_cast<uint4*>(zr + tile_off(lt, k, 128)) = w;
             }
         }
