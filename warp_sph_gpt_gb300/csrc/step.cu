@@ -156,8 +156,11 @@ int fork_for_current_device(Fork** out) {
 //                   grid are ready.
 // build: the step first re-bins its moving grids (the loop body) -- the
 // fluid grid only if !fluid_fresh; the single-call API has built them already.
+// density_fresh (no Shepard step): the sorted copies, densities, pressures and
+// neighbour records of the current positions are in place already (a learned
+// jump's judge computed them), so the gather and the density pass are skipped.
 int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaStream_t st, bool build = false,
-                    bool fluid_fresh = false) {
+                    bool fluid_fresh = false, bool density_fresh = false) {
     Fork* f = nullptr;
     TRY(fork_for_current_device(&f));
     auto rec = [&](cudaEvent_t ev, cudaStream_t s) {
@@ -180,7 +183,7 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
     // main, up to the fork of the porosity branch
     if (build) {
         if (!fluid_fresh) TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
-        TRY(gather_fluid(c, st));
+        if (!density_fresh) TRY(gather_fluid(c, st));
     }
     TRY(run_dem_aux(c, st));
     if (shep) TRY(gather_wall_rho(c, st));
@@ -189,8 +192,9 @@ int coupled_onestep(sphdem_ctx_t* c, const sphdem_params_t* p, bool shep, cudaSt
     TRY(run_density_wall(c, p->support, p->h, true, p->rho0, p->c0, p->gamma, f->side3, p->block_sph, p->lanes_sph));
     TRY(rec(f->wall, f->side3));
     const int cap = nbr_cap(c, p);
-    TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
-                    cap, p->nbr_format));
+    if (!density_fresh)
+        TRY(run_density(c, p->support, p->h, shep, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph,
+                        p->lanes_sph, cap, p->nbr_format));
     TRY(rec(f->dens, st));
     // porosity branch.  One state: what needs positions only (the sorted
     // copies and the DEM grid) runs beside the density pass, the normaliser
@@ -727,9 +731,11 @@ int jump_keep(sphdem_ctx_t* c, const sphdem_jump_t* j, bool restore, cudaStream_
     return launch_status("jump keep");
 }
 
+// dens_fresh: the previous jump's judge (or fallback body) left this state's
+// density pass done (device-judged rollouts).
 int jump_body(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j, bool shep, bool fresh,
-              cudaStream_t st) {
-    TRY(coupled_onestep(c, p, shep, st, true, fresh));
+              cudaStream_t st, bool dens_fresh = false) {
+    TRY(coupled_onestep(c, p, shep, st, true, fresh, dens_fresh && fresh && !shep));
     TRY(jump_keep(c, j, false, st));
     TRY(sphdem_mpnn_nodes(&j->nodes, st));
     sphdem_grid_t g = j->node_grid;
@@ -746,7 +752,10 @@ int jump_body(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_t* j,
     TRY(run_corrmax(j->net.out, c->sph.n, c->dem.n, j->scale, (float)j->substeps * p->dt, j->dev + 1, st));
     TRY(build_grid(&c->grid_sph, c->sph.pos, c->ctl, st));
     TRY(gather_fluid(c, st));
-    TRY(run_density(c, p->support, p->h, false, true, false, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph));
+    // the judge's density is the full density pass of the next plain step
+    // (pressures, sorted copies, neighbour records), so that step can skip it
+    TRY(run_density(c, p->support, p->h, false, true, true, p->rho0, p->c0, p->gamma, st, p->block_sph, p->lanes_sph,
+                    nbr_cap(c, p), p->nbr_format));
     const float* rho_old = j->keep + 6 * (size_t)c->sph.n + 6 * (size_t)c->dem.n;
     return sphdem_mpnn_maxdev(c->sph.rho, j->judge == 1 ? nullptr : rho_old, p->rho0, c->sph.n, 1.0f / p->rho0,
                               j->dev, st);
@@ -853,7 +862,9 @@ int sphdem_jump_undo(sphdem_ctx_t* c, const sphdem_jump_t* j, sphdem_stream_t st
 // device-judged rollout: the jumps are replayed back to back with no host
 // round trip.  Each rollout graph is the jump's graph plus a judge kernel
 // that sets a conditional node: non-zero runs the fallback body (undo the
-// substeps, m plain steps, then the fluid re-bin the next jump relies on).
+// substeps, m plain steps, then the fluid re-bin and density pass the next
+// jump relies on: after any jump of a rollout, the next one's plain step
+// skips both unless its step refreshes the Shepard normaliser).
 // ---------------------------------------------------------------------------
 namespace {
 
@@ -864,8 +875,9 @@ struct RolloutEntry {
     float tol = 0.0f;
     int32_t* stats = nullptr;
     cudaStream_t cap = nullptr;
-    std::map<int, cudaGraphExec_t> exec;            // key: Shepard pattern of the K steps * 2 + fresh
-    std::map<int, std::pair<int, int>> kernels;     // key -> (jump graph, fallback body) kernel nodes
+    // key: Shepard pattern of the K steps and of the next jump's first step, * 2 + fresh
+    std::map<int64_t, cudaGraphExec_t> exec;
+    std::map<int64_t, std::pair<int, int>> kernels;  // key -> (jump graph, fallback body) kernel nodes
 };
 std::map<const sphdem_ctx_t*, RolloutEntry> g_rollouts;
 
@@ -892,7 +904,7 @@ int capture_rollout(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump
     cudaGraphConditionalHandle cond = 0;
     e = cudaStreamGetCaptureInfo(cap, &cs, nullptr, &graph);
     if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&cond, graph, 0, cudaGraphCondAssignDefault);
-    int rc = e == cudaSuccess ? jump_body(c, p, j, shep, fresh, cap) : SPHDEM_ERR_CUDA;
+    int rc = e == cudaSuccess ? jump_body(c, p, j, shep, fresh, cap, fresh) : SPHDEM_ERR_CUDA;
     cudaGraph_t body = nullptr;
     if (!rc) {
         k_decide<<<1, 1, 0, cap>>>(j->dev, j->graph_ctl, tol, j->pos_tol, cond, stats);
@@ -926,6 +938,15 @@ int capture_rollout(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump
     rc = jump_keep(c, j, true, cap);
     for (int s = 1; !rc && s <= j->substeps; ++s) rc = loop_body(c, p, shepard_due(p, step + s), 1, cap);
     if (!rc) rc = build_grid(&c->grid_sph, c->sph.pos, c->ctl, cap);
+    // and the density pass of the next jump's plain step, as a judge leaves it
+    // -- unless that step refreshes the Shepard normaliser: it then runs its
+    // own, from m / rho of this step's density (which must stay in place)
+    if (!rc && !shepard_due(p, step + j->substeps + 1)) {
+        rc = gather_fluid(c, cap);
+        if (!rc)
+            rc = run_density(c, p->support, p->h, false, true, true, p->rho0, p->c0, p->gamma, cap, p->block_sph,
+                             p->lanes_sph, nbr_cap(c, p), p->nbr_format);
+    }
     cudaGraph_t body_done = nullptr;
     e = cudaStreamEndCapture(cap, &body_done);
     if (rc || e != cudaSuccess) {
@@ -969,9 +990,9 @@ int sphdem_rollout(sphdem_ctx_t* c, const sphdem_params_t* p, const sphdem_jump_
     bool fresh = (flags & SPHDEM_JUMP_GRID_FRESH) != 0;
     for (int i = 0; i < n_jumps; ++i) {
         const int step = first_step + i * K;
-        int pattern = 0;
-        for (int s = 0; s < K; ++s) pattern |= shepard_due(p, step + s) ? (1 << s) : 0;
-        const int key = pattern * 2 + (fresh ? 1 : 0);
+        int64_t pattern = 0;
+        for (int s = 0; s <= K; ++s) pattern |= shepard_due(p, step + s) ? (int64_t(1) << s) : 0;
+        const int64_t key = pattern * 2 + (fresh ? 1 : 0);
         auto it = e.exec.find(key);
         if (it == e.exec.end()) {
             cudaGraphExec_t x = nullptr;
@@ -999,8 +1020,9 @@ int64_t sphdem_rollout_kernels(sphdem_ctx_t* c, int first_step, int n_jumps, int
     bool fresh = (flags & SPHDEM_JUMP_GRID_FRESH) != 0;
     int64_t total = 0;
     for (int i = 0; i < n_jumps; ++i) {
-        int pattern = 0;
-        for (int s = 0; s < K; ++s) pattern |= shepard_due(&e.params, first_step + i * K + s) ? (1 << s) : 0;
+        int64_t pattern = 0;
+        for (int s = 0; s <= K; ++s)
+            pattern |= shepard_due(&e.params, first_step + i * K + s) ? (int64_t(1) << s) : 0;
         auto k = e.kernels.find(pattern * 2 + (fresh ? 1 : 0));
         if (k == e.kernels.end()) return -1;
         total += body ? k->second.second : k->second.first;
