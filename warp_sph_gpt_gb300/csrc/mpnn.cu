@@ -102,6 +102,15 @@ __device__ __forceinline__ uint32_t cta_begin(uint64_t* bars, uint32_t* slot, ui
     return *slot;
 }
 
+// The same prologue when thread 0 has already initialised the barriers.
+__device__ __forceinline__ uint32_t cta_tmem(uint32_t* slot, uint32_t ncols) {
+    if ((threadIdx.x >> 5) == 0) umma::tmem_alloc(slot, ncols);
+    umma::fence_before();
+    __syncthreads();
+    umma::fence_after();
+    return *slot;
+}
+
 // Issue (thread 0) after the operand tiles were written and fenced by all.
 __device__ __forceinline__ void operands_ready() {
     fence_proxy_async_smem();
@@ -169,9 +178,8 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
                                              int n_add, const uint16_t* __restrict__ B,
                                              const float* __restrict__ bias, float* __restrict__ out_f32,
                                              uint16_t* __restrict__ out_bf, float* __restrict__ z_out,
-                                             int32_t* status, const int* __restrict__ list, int n_direct) {
-    pdl_wait();
-    pdl_launch();
+                                             int32_t* status, const int* __restrict__ list, int n_direct,
+                                             int early) {
     constexpr uint32_t kB = N * K * 2, kA = kT * K * 2;
     constexpr uint32_t kCols = N < 32 ? 32 : N;
     extern __shared__ __align__(1024) uint8_t sm[];
@@ -182,12 +190,24 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
     uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 2);
     const int tid = threadIdx.x, warp = tid >> 5;
 
-    const uint32_t tmem = cta_begin(bars, slot, kCols);
+    // early (inference): the weight image is fixed, so its copy starts before
+    // the previous kernel is done (no kernel of the inference chain writes it)
+    const bool pre = IMG && early;
+    if (pre && tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_mbar_init();
+        mbar_arrive_expect_tx(&bars[1], kB);
+        tma_load_1d(sB, B, kB, &bars[1]);
+    }
+    pdl_wait();
+    pdl_launch();
+    const uint32_t tmem = pre ? cta_tmem(slot, kCols) : cta_begin(bars, slot, kCols);
     for (int i = tid; i < N; i += kT) sbias[i] = bias ? bias[i] : 0.0f;
     bool mine = true, failed = false, pending = false;
     uint32_t phase = 0;
     if (IMG) {
-        if (tid == 0) {
+        if (tid == 0 && !pre) {
             mbar_arrive_expect_tx(&bars[1], kB);
             tma_load_1d(sB, B, kB, &bars[1]);
         }
@@ -301,6 +321,7 @@ struct EdgeArgs {
     float* dh0;            // [n,128]
     float* partial;        // [grid][kBwdStride]
     int32_t* status;
+    int early;             // inference: the weight images are copied before the previous kernel is done
 };
 
 // Edge features of edge e (zeros past the end): ((x_j-x_i)/R, |x_j-x_i|/R,
@@ -411,8 +432,6 @@ __device__ __forceinline__ bool pipe_or256(bool v, int id) {
 
 template <int MODE>
 __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
-    pdl_wait();
-    pdl_launch();
     extern __shared__ __align__(1024) uint8_t sm[];
     uint8_t* img1 = sm + EF_IMG1;
     uint8_t* img2 = sm + EF_IMG2;
@@ -432,19 +451,25 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
     uint64_t* bar = &bars[p];
     uint64_t* hbar = &bars[3 + p];
     const int bid = 1 + p;
-    const int E = min(__ldg(a.offset + a.n_recv), a.cap);
-
     if (tid == 0) {
         for (int b = 0; b < 5; ++b) mbar_init(&bars[b], 1);
         fence_mbar_init();
+        if (a.early) {  // the weight images are fixed: copy them while the previous kernel drains
+            mbar_arrive_expect_tx(&bars[2], kImg16 + kImg128);
+            tma_load_1d(img1, a.img_e1, kImg16, &bars[2]);
+            tma_load_1d(img2, a.img_e2, kImg128, &bars[2]);
+        }
     }
+    pdl_wait();
+    pdl_launch();
+    const int E = min(__ldg(a.offset + a.n_recv), a.cap);
     if (warp == 0) umma::tmem_alloc(slot, 256);
     if (tid < 128) b2[tid] = a.b2[tid];
     umma::fence_before();
     __syncthreads();
     umma::fence_after();
     const uint32_t tmem = *slot + 128u * p;
-    if (tid == 0) {
+    if (tid == 0 && !a.early) {
         mbar_arrive_expect_tx(&bars[2], kImg16 + kImg128);
         tma_load_1d(img1, a.img_e1, kImg16, &bars[2]);
         tma_load_1d(img2, a.img_e2, kImg128, &bars[2]);
@@ -1177,7 +1202,7 @@ int smem_opt_in(Kern k, uint32_t bytes) {
 template <int K, int N, int EPI, bool IMG>
 int rows(const uint16_t* A, int M, const uint16_t* B, const float* bias, float* out_f32, uint16_t* out_bf,
          float* z_out, int32_t* status, cudaStream_t st, const float* add = nullptr, int n_add = 0,
-         const int* list = nullptr, int n_direct = 0) {
+         const int* list = nullptr, int n_direct = 0, int early = 0) {
     if (M <= 0) return SPHDEM_OK;
     constexpr uint32_t bytes = N * K * 2 + kT * K * 2 + 4 * (N < 2 ? 2 : N) + 16 + 16;
     int rc = smem_opt_in(k_rows<K, N, EPI, IMG>, bytes);
@@ -1185,7 +1210,7 @@ int rows(const uint16_t* A, int M, const uint16_t* B, const float* bias, float* 
     const int tiles = (M + kT - 1) / kT;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
     launch_pdl(k_rows<K, N, EPI, IMG>, grid, kT, bytes, st, A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status, list,
-                                                    n_direct);
+                                                    n_direct, early);
     return launch_status("mpnn rows");
 }
 
@@ -1363,9 +1388,14 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
         list = n->active_list;
     }
     int rc = rows<16, 128, EPI_SILU, true>(n->x, nn, n->packed + P_N1, n->theta + SPHDEM_MPNN_N1_B, nullptr, n->h0,
-                                           store_pre ? n->z0 : nullptr, n->status, st, nullptr, 0, list, nr);
+                                           store_pre ? n->z0 : nullptr, n->status, st, nullptr, 0, list, nr,
+                                           list != nullptr);
     if (rc) return rc;
+    // Inference copies the weight images early: every kernel of the chain
+    // runs behind kernels that do not write them (the first node layer only
+    // behind the sender marking, which itself waits on whatever packed them).
     EdgeArgs a = edge_args(n);
+    a.early = !store_pre;
     const int eg = edge_grid(n, 1);
     for (int round = 0; round < 2; ++round) {
         cudaError_t e = zero_words(n->agg, (long)nr * kH, st);
@@ -1383,7 +1413,7 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
                                                     nullptr, n->h2, n->z2, n->status, st);
             } else {  // h1 = h0 + agg formed while staging
                 rc = rows<128, 128, EPI_SILU, true>(n->h0, nn, n->packed + P_N2, n->theta + SPHDEM_MPNN_N2_B,
-                                                    nullptr, n->h2, nullptr, n->status, st, n->agg, nr, list, nr);
+                                                    nullptr, n->h2, nullptr, n->status, st, n->agg, nr, list, nr, 1);
             }
             if (rc) return rc;
         } else if (store_pre) {
@@ -1395,7 +1425,7 @@ extern "C" int sphdem_mpnn_forward(const sphdem_mpnn_net_t* n, int store_pre, sp
                                           nullptr, n->status, st);
     else
         rc = rows<128, 16, EPI_F32, true>(n->h2, nr, n->packed + P_N3, n->theta + SPHDEM_MPNN_N3_B, n->out, nullptr,
-                                          nullptr, n->status, st, n->agg, nr);
+                                          nullptr, n->status, st, n->agg, nr, nullptr, 0, 1);
     if (rc) return rc;
     return launch_status("mpnn_forward");
 }
