@@ -174,7 +174,7 @@ __global__ void k_pack(const float* __restrict__ theta, uint16_t* __restrict__ p
 // list (optional): the layer runs on rows 0 .. n_direct - 1 and on the list[0]
 // rows list[1 ..] (in any order: rows are independent); M bounds both.
 template <int K, int N, int EPI, bool IMG>
-__global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int M, const float* __restrict__ add,
+__global__ void __launch_bounds__(2 * kT) k_rows(const uint16_t* __restrict__ A, int M, const float* __restrict__ add,
                                              int n_add, const uint16_t* __restrict__ B,
                                              const float* __restrict__ bias, float* __restrict__ out_f32,
                                              uint16_t* __restrict__ out_bf, float* __restrict__ z_out,
@@ -188,7 +188,10 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
     float* sbias = reinterpret_cast<float*>(sA + kA);
     uint64_t* bars = reinterpret_cast<uint64_t*>(sbias + (N < 2 ? 2 : N));
     uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 2);
-    const int tid = threadIdx.x, warp = tid >> 5;
+    // two threads per row: thread rt and rt + kT stage half of row rt's
+    // chunks each, and the warps w and w + 4 (same TMEM lanes) split the
+    // output columns
+    const int tid = threadIdx.x, warp = tid >> 5, rt = tid & (kT - 1), hh = tid / kT;
 
     // early (inference): the weight image is fixed, so its copy starts before
     // the previous kernel is done (no kernel of the inference chain writes it)
@@ -203,7 +206,7 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
     pdl_wait();
     pdl_launch();
     const uint32_t tmem = pre ? cta_tmem(slot, kCols) : cta_begin(bars, slot, kCols);
-    for (int i = tid; i < N; i += kT) sbias[i] = bias ? bias[i] : 0.0f;
+    for (int i = tid; i < N; i += 2 * kT) sbias[i] = bias ? bias[i] : 0.0f;
     bool mine = true, failed = false, pending = false;
     uint32_t phase = 0;
     if (IMG) {
@@ -213,7 +216,7 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
         }
         failed = __syncthreads_or(!mbar_wait(&bars[1], 0, kPolls));
     } else {
-        for (int idx = tid; idx < N * (K / 8); idx += kT) {
+        for (int idx = tid; idx < N * (K / 8); idx += 2 * kT) {
             const int r = idx / (K / 8), q = idx % (K / 8);
             *reinterpret_cast<uint4*>(sB + tile_off(r, 8 * q, K)) =
                 __ldg(reinterpret_cast<const uint4*>(B + (size_t)r * K) + q);
@@ -223,11 +226,11 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
     constexpr uint32_t idesc = umma::idesc_bf16(128, N);
     const int Mv = list ? min(M, n_direct + __ldg(list)) : M;  // rows of this launch
     for (int tile = blockIdx.x; !failed && tile * kT < Mv; tile += gridDim.x) {
-        int row = tile * kT + tid;
+        int row = tile * kT + rt;
         if (list && row >= n_direct) row = row < Mv ? __ldg(list + 1 + (row - n_direct)) : M;  // M: no row
         const bool plus = add != nullptr && row < n_add;
 #pragma unroll
-        for (int q = 0; q < K / 8; ++q) {
+        for (int q = hh * (K / 16); q < (hh + 1) * (K / 16); ++q) {
             uint4 v = make_uint4(0, 0, 0, 0);
             if (row < M) v = __ldg(reinterpret_cast<const uint4*>(A + (size_t)row * K) + q);
             if (plus) {
@@ -238,7 +241,7 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
                                pack2(bf((uint16_t)v.z) + a1.x, bf((uint16_t)(v.z >> 16)) + a1.y),
                                pack2(bf((uint16_t)v.w) + a1.z, bf((uint16_t)(v.w >> 16)) + a1.w));
             }
-            *reinterpret_cast<uint4*>(sA + tile_off(tid, 8 * q, K)) = v;
+            *reinterpret_cast<uint4*>(sA + tile_off(rt, 8 * q, K)) = v;
         }
         operands_ready();
         if (tid == 0) {
@@ -252,14 +255,15 @@ __global__ void __launch_bounds__(kT) k_rows(const uint16_t* __restrict__ A, int
             break;
         }
         pending = false;
+        // columns of this thread: [hh N/2, hh N/2 + N/2), or all 16 (thread rt) when N = 16
+        constexpr int W = N < 32 ? 16 : 32, NH = N < 32 ? N : N / 2;
 #pragma unroll
-        for (int c0 = 0; c0 < N; c0 += (N < 32 ? 16 : 32)) {
+        for (int c0 = hh * NH; c0 < hh * NH + NH && c0 < N; c0 += W) {
             float v[32];
             if (N < 32)
-                umma::tmem_ld16(umma::taddr(tmem, 32 * warp, c0), v);
+                umma::tmem_ld16(umma::taddr(tmem, 32 * (warp & 3), c0), v);
             else
-                umma::tmem_ld32(umma::taddr(tmem, 32 * warp, c0), v);
-            constexpr int W = N < 32 ? 16 : 32;
+                umma::tmem_ld32(umma::taddr(tmem, 32 * (warp & 3), c0), v);
             if (row < M) {
                 if (EPI == EPI_F32) {
                     float4* o = reinterpret_cast<float4*>(out_f32 + (size_t)row * N + c0);
@@ -475,7 +479,7 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
         tma_load_1d(img2, a.img_e2, kImg128, &bars[2]);
     }
     bool failed = __syncthreads_or(!mbar_wait(&bars[2], 0, kPolls));
-    bool mine = true, pending = false, hpending = false;
+    bool mine = true, hmine = true, pending = false, hpending = false;
     uint32_t phase = 0, hphase = 0;
     constexpr uint32_t idesc = umma::idesc_bf16(128, 128);
     const int stride = 2 * gridDim.x;
@@ -520,10 +524,13 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
         }
         if (MODE == MODE_AGG) hpending = true;
         pending = true;
+        // A wait that gives up is reported at the pipeline's next barrier,
+        // which then reduces the outcome (what is read meanwhile is discarded).
         mine = mbar_wait(bar, phase, kPolls);
-        if (pipe_or256(!mine, bid)) { failed = true; break; }
-        phase ^= 1u;
-        pending = false;
+        if (mine) {
+            phase ^= 1u;
+            pending = false;
+        }
         umma::fence_after();
         // layer-1 epilogue: lane = edge, this half's 64 hidden units
 #pragma unroll
@@ -543,7 +550,7 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
         }
         fence_proxy_async_smem();
         umma::fence_before();
-        pipe_sync256(bid);
+        if (pipe_or256(!mine, bid)) { failed = true; break; }
         if (plt == 0) {
             umma::fence_after();
             umma::mma_tile(tmem, img2, zr, 128, idesc, false);  // D[c][e], over layer 1's columns
@@ -552,35 +559,49 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
         if (loader) edge_load_state(a, nxt);  // the next tile's particle state
         pending = true;
         mine = mbar_wait(bar, phase, kPolls);
-        if (pipe_or256(!mine, bid)) { failed = true; break; }
-        phase ^= 1u;
-        pending = false;
+        if (mine) {
+            phase ^= 1u;
+            pending = false;
+        }
         umma::fence_after();
         // layer-2 epilogue: lane = feature c, this half's 64 edges of the tile
         const int c = lt;
         const float bc = b2[c];
         int cur = -1;
-        float acc = 0.0f, gval = 0.0f;
+        float gval = 0.0f;
         if (MODE == MODE_AGG) {
-            const bool hmine = mbar_wait(hbar, hphase, kPolls);
-            if (pipe_or256(!hmine, bid)) { failed = true; break; }
-            hphase ^= 1u;
-            hpending = false;
+            hmine = mbar_wait(hbar, hphase, kPolls);
+            if (hmine) {
+                hphase ^= 1u;
+                hpending = false;
+            }
             const uint16_t* h16 = reinterpret_cast<const uint16_t*>(hs) + c;
             const uint32_t* ends = reinterpret_cast<const uint32_t*>(pb + EF_P_END);
+            // Segmented sums over the receiver-sorted edges; a group of 8
+            // edges that ends no run (most of them: ~30 edges per receiver)
+            // runs without the per-edge flush tests.
+            float acc = 0.0f;
 #pragma unroll 1
             for (int c0 = 64 * half; c0 < 64 * half + 64; c0 += 32) {
                 float v[32];
                 umma::tmem_ld32(umma::taddr(tmem, lanes, c0), v);
-                const uint32_t em = ends[c0 >> 5];
+                const uint32_t em = ends[c0 >> 5];  // warp-uniform: the same edges end a run for every feature
 #pragma unroll
-                for (int i = 0; i < 32; ++i) {
-                    const float t = fmaf(v[i] + bc, bf(h16[(c0 + i) * kH]), acc);
-                    if (em & (1u << i)) {  // warp-uniform: the same edges end a run for every feature
-                        atomicAdd(a.agg + (size_t)sr[c0 + i] * kH + c, t * a.inv_norm);
-                        acc = 0.0f;
+                for (int g = 0; g < 32; g += 8) {
+                    if (((em >> g) & 0xffu) == 0u) {
+#pragma unroll
+                        for (int i = g; i < g + 8; ++i) acc = fmaf(v[i] + bc, bf(h16[(c0 + i) * kH]), acc);
                     } else {
-                        acc = t;
+#pragma unroll
+                        for (int i = g; i < g + 8; ++i) {
+                            const float t = fmaf(v[i] + bc, bf(h16[(c0 + i) * kH]), acc);
+                            if (em & (1u << i)) {
+                                atomicAdd(a.agg + (size_t)sr[c0 + i] * kH + c, t * a.inv_norm);
+                                acc = 0.0f;
+                            } else {
+                                acc = t;
+                            }
+                        }
                     }
                 }
             }
@@ -602,7 +623,7 @@ __global__ void __launch_bounds__(2 * kPT, 1) k_edges(EdgeArgs a) {
             }
         }
         umma::fence_before();
-        pipe_sync256(bid);
+        if (pipe_or256(!mine || !hmine, bid)) { failed = true; break; }
     }
     if (failed && plt == 0) raise_flag(a.status, SPHDEM_FLAG_TIMEOUT);
     if (pending && !mine) mbar_wait(bar, phase, kPolls);
@@ -1209,7 +1230,7 @@ int rows(const uint16_t* A, int M, const uint16_t* B, const float* bias, float* 
     if (rc) return rc;
     const int tiles = (M + kT - 1) / kT;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-    launch_pdl(k_rows<K, N, EPI, IMG>, grid, kT, bytes, st, A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status, list,
+    launch_pdl(k_rows<K, N, EPI, IMG>, grid, 2 * kT, bytes, st, A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status, list,
                                                     n_direct, early);
     return launch_status("mpnn rows");
 }
