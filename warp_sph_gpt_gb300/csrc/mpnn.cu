@@ -41,6 +41,7 @@ using umma::tile_off;
 
 constexpr int kH = SPHDEM_MPNN_HIDDEN;
 constexpr int kT = 128;  // threads per CTA = rows per tile
+constexpr int kRT = 4;   // node layers: threads per row (kRT x kT threads per CTA)
 constexpr int kPolls = 1 << 20;
 constexpr int kMaxCtas = 512;
 constexpr int kBwdStride = 128 * 128 + 128 * 16 + 256;  // per-CTA partials of k_edges_bwd
@@ -174,7 +175,7 @@ __global__ void k_pack(const float* __restrict__ theta, uint16_t* __restrict__ p
 // list (optional): the layer runs on rows 0 .. n_direct - 1 and on the list[0]
 // rows list[1 ..] (in any order: rows are independent); M bounds both.
 template <int K, int N, int EPI, bool IMG>
-__global__ void __launch_bounds__(2 * kT) k_rows(const uint16_t* __restrict__ A, int M, const float* __restrict__ add,
+__global__ void __launch_bounds__(kRT * kT) k_rows(const uint16_t* __restrict__ A, int M, const float* __restrict__ add,
                                              int n_add, const uint16_t* __restrict__ B,
                                              const float* __restrict__ bias, float* __restrict__ out_f32,
                                              uint16_t* __restrict__ out_bf, float* __restrict__ z_out,
@@ -188,8 +189,8 @@ __global__ void __launch_bounds__(2 * kT) k_rows(const uint16_t* __restrict__ A,
     float* sbias = reinterpret_cast<float*>(sA + kA);
     uint64_t* bars = reinterpret_cast<uint64_t*>(sbias + (N < 2 ? 2 : N));
     uint32_t* slot = reinterpret_cast<uint32_t*>(bars + 2);
-    // two threads per row: thread rt and rt + kT stage half of row rt's
-    // chunks each, and the warps w and w + 4 (same TMEM lanes) split the
+    // kRT threads per row: threads rt + i kT stage a share of row rt's
+    // 16-byte chunks, and warps w, w + 4, ... (same TMEM lanes) split the
     // output columns
     const int tid = threadIdx.x, warp = tid >> 5, rt = tid & (kT - 1), hh = tid / kT;
 
@@ -206,7 +207,7 @@ __global__ void __launch_bounds__(2 * kT) k_rows(const uint16_t* __restrict__ A,
     pdl_wait();
     pdl_launch();
     const uint32_t tmem = pre ? cta_tmem(slot, kCols) : cta_begin(bars, slot, kCols);
-    for (int i = tid; i < N; i += 2 * kT) sbias[i] = bias ? bias[i] : 0.0f;
+    for (int i = tid; i < N; i += kRT * kT) sbias[i] = bias ? bias[i] : 0.0f;
     bool mine = true, failed = false, pending = false;
     uint32_t phase = 0;
     if (IMG) {
@@ -216,7 +217,7 @@ __global__ void __launch_bounds__(2 * kT) k_rows(const uint16_t* __restrict__ A,
         }
         failed = __syncthreads_or(!mbar_wait(&bars[1], 0, kPolls));
     } else {
-        for (int idx = tid; idx < N * (K / 8); idx += 2 * kT) {
+        for (int idx = tid; idx < N * (K / 8); idx += kRT * kT) {
             const int r = idx / (K / 8), q = idx % (K / 8);
             *reinterpret_cast<uint4*>(sB + tile_off(r, 8 * q, K)) =
                 __ldg(reinterpret_cast<const uint4*>(B + (size_t)r * K) + q);
@@ -229,8 +230,9 @@ __global__ void __launch_bounds__(2 * kT) k_rows(const uint16_t* __restrict__ A,
         int row = tile * kT + rt;
         if (list && row >= n_direct) row = row < Mv ? __ldg(list + 1 + (row - n_direct)) : M;  // M: no row
         const bool plus = add != nullptr && row < n_add;
+        constexpr int CPT = K / 8 < kRT ? 1 : K / 8 / kRT;  // chunks per thread
 #pragma unroll
-        for (int q = hh * (K / 16); q < (hh + 1) * (K / 16); ++q) {
+        for (int q = hh * CPT; q < hh * CPT + CPT && q < K / 8; ++q) {
             uint4 v = make_uint4(0, 0, 0, 0);
             if (row < M) v = __ldg(reinterpret_cast<const uint4*>(A + (size_t)row * K) + q);
             if (plus) {
@@ -255,8 +257,9 @@ __global__ void __launch_bounds__(2 * kT) k_rows(const uint16_t* __restrict__ A,
             break;
         }
         pending = false;
-        // columns of this thread: [hh N/2, hh N/2 + N/2), or all 16 (thread rt) when N = 16
-        constexpr int W = N < 32 ? 16 : 32, NH = N < 32 ? N : N / 2;
+        // columns of this thread: [hh NH, hh NH + NH), or all 16 (thread rt) when N = 16
+        constexpr int W = N < 32 ? 16 : 32, NH = N < 32 ? N : N / kRT;
+        static_assert(N < 32 || NH % 32 == 0, "k_rows column split");
 #pragma unroll
         for (int c0 = hh * NH; c0 < hh * NH + NH && c0 < N; c0 += W) {
             float v[32];
@@ -1230,8 +1233,8 @@ int rows(const uint16_t* A, int M, const uint16_t* B, const float* bias, float* 
     if (rc) return rc;
     const int tiles = (M + kT - 1) / kT;
     const int grid = tiles < 2 * sm_count() ? tiles : 2 * sm_count();
-    launch_pdl(k_rows<K, N, EPI, IMG>, grid, 2 * kT, bytes, st, A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status, list,
-                                                    n_direct, early);
+    launch_pdl(k_rows<K, N, EPI, IMG>, grid, kRT * kT, bytes, st, A, M, add, n_add, B, bias, out_f32, out_bf, z_out, status,
+               list, n_direct, early);
     return launch_status("mpnn rows");
 }
 
