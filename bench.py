@@ -896,7 +896,7 @@ def main():
     ap.add_argument("--rollout-steps", type=int, default=1000, help="learned: steps of the compared rollouts")
     ap.add_argument("--judge-tol", type=float, default=0.01, help="learned: density judge tolerance / rho0")
     ap.add_argument("--seed", type=int, default=0, help="learned: seed of the network's initial weights and sampling")
-    ap.add_argument("--pos-tol-dx", type=float, default=0.005,
+    ap.add_argument("--pos-tol-dx", type=float, default=0.0045,
                     help="learned: position judge -- fall back when the network's correction would move a particle "
                          "more than this many dx beyond the constant-acceleration prior within one jump (0 = off)")
     ap.add_argument("--ema", type=float, default=0.0, help="learned: parameter moving-average decay (0 = off)")
