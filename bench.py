@@ -831,8 +831,10 @@ def reference_arm(args):
         steps.append(cpu_sample(host, solv, scales, stride, 1 + args.warmup + s) * scale)
     step_s = statistics.mean(steps)
     value = n_units / step_s
-    timing = (f"step 1 of {args.steps} timed in full ({t_full:.2f} s, every subject); steps 2-{args.steps} on "
-              f"every {stride}-th subject, scaled by the measured full/sample ratio {scale:.2f}")
+    timing = f"step 1 of {args.steps} timed in full ({t_full:.2f} s, every subject)"
+    if args.steps > 1:
+        timing += (f"; steps 2-{args.steps} on every {stride}-th subject, scaled by the measured full/sample "
+                   f"ratio {scale:.2f}")
     return {"impl": "reference", "metric": "particle-steps/s", "value": value, "unit": "particle-steps/s",
             "n_gpus": 0, "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_s * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",

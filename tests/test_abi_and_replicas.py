@@ -5,6 +5,8 @@
   have the library's own sizes.
 * bench.py --gpus N runs N independent replicas (the step does not shard);
   the job time is the max over ranks, checked here with two gloo ranks.
+* bench.py --impl reference (the reference algorithm on the host cores) prints
+  one JSON line with the bench contract's keys, on the small dam break.
 """
 import ctypes as C
 import os
@@ -96,3 +98,23 @@ def test_single_rank_is_identity():
 
     assert bench.reduce_max(7.5, 1) == 7.5
     assert bench.job_throughput(100, 4, 1, 2.0) == pytest.approx(200000.0)
+
+
+def test_reference_arm_line_on_host():
+    import json
+    import subprocess
+
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--workload", "small",
+                          "--steps", "2", "--warmup", "3", "--cpu-budget-s", "2"],
+                         capture_output=True, text=True, cwd=ROOT, timeout=600)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [l for l in out.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["metric"] == "particle-steps/s" and d["higher_is_better"] is True
+    assert d["steps"] == 2 and d["warmup"] >= 3 and d["value"] > 0
+    assert d["value"] == pytest.approx((d["config"]["fluid"] + d["config"]["dem"]) / (d["ms_per_step"] * 1e-3))
+    cb = d["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert cb["measured"]["steps_timed_in_full"] == 1
+    assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
